@@ -1,0 +1,515 @@
+// Schedule builder: grammar (or the reference's proper-layered schedule) ->
+// level-major, child-sorted plan for the GB300 sweep.
+//
+// The reference lays a grammar out in levels (build_schedule.cpp:57-71:
+// lvl(N -> A B) = 1 + max(lvl A, lvl B), terminals at 0), inserts identity
+// pass-through nodes so every child sits in the frontier directly below its
+// parent (build_schedule.cpp:119-135), emits each non-terminal occurrence
+// of C at the symbol's own level (build_schedule.cpp:138-155) and compacts
+// the terminal alphabet to the referenced ones (build_schedule.cpp:187-224).
+//
+// The plan keeps the levels, the emit-at-own-level rule and the compacted
+// terminals, and changes the layout:
+//   * all values of one multiply live in one arena (one slot per evaluated
+//     rule, level-major), so a pass-through is a reference to its source
+//     slot instead of a copied value: no pass-through work at run time;
+//   * within a level, rules are sorted by (left child, right child), so the
+//     left-child gathers of consecutive threads are monotone;
+//   * emissions of a level are sorted by (row, source), so a warp reduces a
+//     row segment in registers and issues one atomic per segment;
+//   * ops and emissions are structure-of-arrays (8 bytes per binary rule,
+//     the coefficient array exists only when a run-length rule does).
+// The reference's own layered figures (L, w*, |R|, +pt, E, E_T, U) are
+// computed alongside for reporting and for the roofline byte count.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <numeric>
+
+#include "gmr_internal.h"
+
+namespace gmr {
+
+namespace {
+
+// Level index of an arena slot (binary search over level offsets).
+int level_of_slot(const std::vector<int64_t>& lvl_off, int64_t slot) {
+    // lvl_off[k] = end of level k; level k covers [lvl_off[k-1], lvl_off[k]).
+    auto it = std::upper_bound(lvl_off.begin(), lvl_off.end(), slot);
+    return (int)(it - lvl_off.begin());
+}
+
+// Sort ops of one level by (left, right) and return the permutation.
+std::vector<int64_t> child_sort(const std::vector<int32_t>& L, const std::vector<int32_t>& R) {
+    std::vector<int64_t> perm(L.size());
+    std::iota(perm.begin(), perm.end(), 0);
+    std::sort(perm.begin(), perm.end(), [&](int64_t a, int64_t b) {
+        if (L[a] != L[b]) return L[a] < L[b];
+        if (R[a] != R[b]) return R[a] < R[b];
+        return a < b;
+    });
+    return perm;
+}
+
+// Group emissions by level, then sort each level's segment by (row, src).
+void finish_emissions(gmr_plan& p, std::vector<int32_t>& lvl_of_em, std::vector<int32_t>& src,
+                      std::vector<int32_t>& row) {
+    const int D = p.depth;
+    std::vector<int64_t> cnt(D + 2, 0);
+    for (int32_t l : lvl_of_em) cnt[l + 1]++;
+    for (int k = 0; k <= D; ++k) cnt[k + 1] += cnt[k];
+    p.em_off = cnt;
+    const int64_t E = (int64_t)src.size();
+    p.em_src.assign(E, 0);
+    p.em_row.assign(E, 0);
+    std::vector<int64_t> pos(cnt.begin(), cnt.end() - 1);
+    for (int64_t e = 0; e < E; ++e) {
+        int64_t d = pos[lvl_of_em[e]]++;
+        p.em_src[d] = src[e];
+        p.em_row[d] = row[e];
+    }
+    // rows are visited in order, so each level segment is row-nondecreasing;
+    // sort sources within each (level, row) group.
+    std::vector<uint64_t> key;
+    for (int k = 0; k <= D; ++k) {
+        int64_t a = p.em_off[k], b = p.em_off[k + 1];
+        int64_t i = a;
+        while (i < b) {
+            int64_t j = i + 1;
+            while (j < b && p.em_row[j] == p.em_row[i]) ++j;
+            if (j - i > 1) std::sort(p.em_src.begin() + i, p.em_src.begin() + j);
+            i = j;
+        }
+        // guard: rows must be non-decreasing inside the level
+        for (int64_t e = a + 1; e < b; ++e)
+            if (p.em_row[e] < p.em_row[e - 1]) {
+                // not row-sorted (caller-supplied emission order): full sort
+                key.resize((size_t)(b - a));
+                for (int64_t q = a; q < b; ++q)
+                    key[q - a] = ((uint64_t)(uint32_t)p.em_row[q] << 32) | (uint32_t)p.em_src[q];
+                std::sort(key.begin(), key.end());
+                for (int64_t q = a; q < b; ++q) {
+                    p.em_row[q] = (int32_t)(key[q - a] >> 32);
+                    p.em_src[q] = (int32_t)(key[q - a] & 0xffffffffu);
+                }
+                break;
+            }
+    }
+}
+
+void fill_common_stats(gmr_plan& p) {
+    auto& s = p.stats;
+    s.rows = p.rows;
+    s.cols = p.cols;
+    s.depth = p.depth;
+    s.n_vals = (int)p.V.size();
+    s.has_coeff = p.has_coeff() ? 1 : 0;
+    s.n_ops = p.n_ops();
+    s.n_terms = p.n_terms();
+    s.n_term_emit = p.em_off.size() > 1 ? p.em_off[1] - p.em_off[0] : 0;
+    s.n_emit = (int64_t)p.em_src.size() - s.n_term_emit;
+    int64_t mx = 0;
+    for (int k = 1; k <= p.depth; ++k) mx = std::max(mx, p.lvl_off[k] - p.lvl_off[k - 1]);
+    s.max_level_ops = mx;
+}
+
+}  // namespace
+
+void validate_plan(const gmr_plan& p) {
+    const int D = p.depth;
+    if ((int)p.lvl_off.size() != D + 1 || p.lvl_off[0] != 0 || p.lvl_off[D] != p.n_ops())
+        throw Error(GMR_ERR_FORMAT, "plan: bad level offsets");
+    if ((int)p.em_off.size() != D + 2 || p.em_off[0] != 0 || p.em_off[D + 1] != (int64_t)p.em_src.size())
+        throw Error(GMR_ERR_FORMAT, "plan: bad emission offsets");
+    const int64_t U = p.n_terms();
+    for (int k = 1; k <= D; ++k) {
+        if (p.lvl_off[k] < p.lvl_off[k - 1]) throw Error(GMR_ERR_FORMAT, "plan: level offsets decrease");
+        for (int64_t i = p.lvl_off[k - 1]; i < p.lvl_off[k]; ++i) {
+            for (int32_t c : {p.op_l[i], p.op_r[i]}) {
+                if (c >= 0 ? (int64_t)c >= p.lvl_off[k - 1] : (int64_t)(-(int64_t)c - 1) >= U)
+                    throw Error(GMR_ERR_FORMAT, "plan: op " + std::to_string(i) + " child " +
+                                                    std::to_string(c) + " out of range");
+            }
+        }
+    }
+    for (int k = 0; k <= D; ++k) {
+        int64_t lo = k == 0 ? 0 : p.lvl_off[k - 1], hi = k == 0 ? 0 : p.lvl_off[k];
+        for (int64_t e = p.em_off[k]; e < p.em_off[k + 1]; ++e) {
+            int32_t c = p.em_src[e];
+            bool ok = c >= 0 ? (c >= lo && c < hi) : (int64_t)(-(int64_t)c - 1) < U;
+            if (k == 0 && c >= 0) ok = false;
+            if (!ok) throw Error(GMR_ERR_FORMAT, "plan: emission source out of range");
+            if (p.em_row[e] < 0 || p.em_row[e] >= p.rows) throw Error(GMR_ERR_FORMAT, "plan: emission row out of range");
+        }
+    }
+    for (size_t q = 0; q < p.term_val.size(); ++q) {
+        if (p.term_val[q] < 0 || p.term_val[q] >= (int32_t)p.V.size())
+            throw Error(GMR_ERR_FORMAT, "plan: terminal value index out of range");
+        if (p.term_col[q] < 0 || p.term_col[q] >= p.cols)
+            throw Error(GMR_ERR_FORMAT, "plan: terminal column out of range");
+    }
+}
+
+}  // namespace gmr
+
+using namespace gmr;
+
+extern "C" int gmr_plan_build(const gmr_grammar* g, int rows, int cols, gmr_plan** out) {
+    return guarded([&] {
+        if (!g || !out || rows < 0 || cols < 1) throw Error(GMR_ERR_ARG, "bad argument");
+        const int32_t alpha = g->alpha;
+        const int64_t n = g->n_rules();
+        const int64_t nv = (int64_t)g->V.size();
+        const int32_t* R = g->rules.data();
+        auto is_rl = [&](int64_t i) { return g->kinds[i] == 1; };
+
+        // (1) levels (build_schedule.cpp:57-71)
+        std::vector<int32_t> lvl((size_t)n, 0);
+        int depth = 0;
+        auto clvl = [&](int32_t s) { return s >= alpha ? lvl[s - alpha] : 0; };
+        for (int64_t i = 0; i < n; ++i) {
+            int l = clvl(R[2 * i]);
+            if (!is_rl(i)) l = std::max(l, clvl(R[2 * i + 1]));
+            lvl[i] = l + 1;
+            depth = std::max(depth, l + 1);
+        }
+
+        auto p = std::make_unique<gmr_plan>();
+        p->rows = rows;
+        p->cols = cols;
+        p->depth = depth;
+        p->V.assign(g->V.begin(), g->V.end());
+
+        // (2) reference-equivalent layered figures on the full grammar
+        {
+            std::vector<int32_t> mref(lvl);
+            for (int64_t i = 0; i < n; ++i) {
+                int32_t l = R[2 * i], r = R[2 * i + 1];
+                if (l >= alpha) mref[l - alpha] = std::max(mref[l - alpha], lvl[i]);
+                if (!is_rl(i) && r >= alpha) mref[r - alpha] = std::max(mref[r - alpha], lvl[i]);
+            }
+            int64_t pt = 0;
+            for (int64_t i = 0; i < n; ++i) pt += mref[i] - lvl[i];
+            // width of reference level k = raw rules of level k + symbols carried
+            // through it (present at levels lvl+1 .. mref as pass-throughs)
+            std::vector<int64_t> raw(depth + 2, 0), diff(depth + 2, 0);
+            for (int64_t i = 0; i < n; ++i) raw[lvl[i]]++;
+            for (int64_t i = 0; i < n; ++i)
+                if (mref[i] > lvl[i]) {
+                    diff[lvl[i] + 1]++;
+                    diff[mref[i] + 1]--;
+                }
+            int64_t run = 0, wmax = 0;
+            for (int k = 1; k <= depth; ++k) {
+                run += diff[k];
+                wmax = std::max(wmax, raw[k] + run);
+            }
+            std::vector<uint8_t> used_t((size_t)alpha, 0);
+            for (int64_t i = 0; i < n; ++i) {
+                if (R[2 * i] < alpha) used_t[R[2 * i]] = 1;
+                if (!is_rl(i) && R[2 * i + 1] < alpha) used_t[R[2 * i + 1]] = 1;
+            }
+            int64_t e = 0, et = 0;
+            for (int32_t c : g->C) {
+                if (c == 0) continue;
+                if (c < alpha) {
+                    ++et;
+                    used_t[c] = 1;
+                } else {
+                    ++e;
+                }
+            }
+            int64_t U = 1;
+            for (int32_t t = 1; t < alpha; ++t) U += used_t[t];
+            auto& s = p->stats;
+            s.ref_raw = n;
+            s.ref_passthrough = pt;
+            s.ref_layered = n + pt;
+            s.ref_max_width = wmax;
+            s.ref_emit = e;
+            s.ref_term_emit = et;
+            s.ref_alpha = U;
+        }
+
+        // (3) live rules: reachable from C
+        std::vector<uint8_t> live((size_t)n, 0);
+        for (int32_t c : g->C)
+            if (c >= alpha) live[c - alpha] = 1;
+        for (int64_t i = n - 1; i >= 0; --i) {
+            if (!live[i]) continue;
+            int32_t l = R[2 * i], r = R[2 * i + 1];
+            if (l >= alpha) live[l - alpha] = 1;
+            if (!is_rl(i) && r >= alpha) live[r - alpha] = 1;
+        }
+
+        // (4) compacted terminals (ascending original code, zero terminal = 0)
+        std::vector<int32_t> tmap((size_t)alpha, 0);
+        for (int64_t i = 0; i < n; ++i) {
+            if (!live[i]) continue;
+            if (R[2 * i] < alpha) tmap[R[2 * i]] = 1;
+            if (!is_rl(i) && R[2 * i + 1] < alpha) tmap[R[2 * i + 1]] = 1;
+        }
+        for (int32_t c : g->C)
+            if (c > 0 && c < alpha) tmap[c] = 1;
+        int32_t U = 1;
+        for (int32_t t = 1; t < alpha; ++t) {
+            if (!tmap[t]) continue;
+            tmap[t] = U++;
+            int64_t vi = (int64_t)(t - 1) / cols, ci = (int64_t)(t - 1) % cols;
+            if (vi >= nv) throw Error(GMR_ERR_FORMAT, "terminal " + std::to_string(t) + " has no value");
+            p->term_val.push_back((int32_t)vi);
+            p->term_col.push_back((int32_t)ci);
+        }
+
+        // (5) slots, level by level, child-sorted
+        std::vector<std::vector<int64_t>> by_level(depth + 1);
+        for (int64_t i = 0; i < n; ++i)
+            if (live[i]) by_level[lvl[i]].push_back(i);
+        std::vector<int32_t> slot((size_t)n, -1);
+        auto ref = [&](int32_t s) -> int32_t { return s >= alpha ? slot[s - alpha] : -tmap[s] - 1; };
+        p->lvl_off.assign(depth + 1, 0);
+        bool coeff = g->has_runlen;
+        int64_t next = 0;
+        for (int k = 1; k <= depth; ++k) {
+            auto& ids = by_level[k];
+            std::vector<int32_t> L(ids.size()), Rr(ids.size());
+            for (size_t j = 0; j < ids.size(); ++j) {
+                int64_t i = ids[j];
+                L[j] = ref(R[2 * i]);
+                Rr[j] = is_rl(i) ? -1 : ref(R[2 * i + 1]);
+            }
+            auto perm = child_sort(L, Rr);
+            if (next + (int64_t)ids.size() > INT32_MAX) throw Error(GMR_ERR_RANGE, "more than 2^31 ops");
+            for (size_t j = 0; j < perm.size(); ++j) {
+                int64_t i = ids[perm[j]];
+                slot[i] = (int32_t)(next + (int64_t)j);
+                p->op_l.push_back(L[perm[j]]);
+                p->op_r.push_back(Rr[perm[j]]);
+                if (coeff) p->op_c.push_back(is_rl(i) ? (float)g->reps[i] : 1.0f);
+            }
+            next += (int64_t)ids.size();
+            p->lvl_off[k] = next;
+            std::vector<int64_t>().swap(ids);
+        }
+
+        // (6) emissions from C at the symbol's own level
+        std::vector<int32_t> el, es, er;
+        el.reserve(g->C.size());
+        es.reserve(g->C.size());
+        er.reserve(g->C.size());
+        int32_t row = 0;
+        for (int32_t c : g->C) {
+            if (c == 0) {
+                ++row;
+                continue;
+            }
+            if (row >= rows) throw Error(GMR_ERR_FORMAT, "C holds more rows than rows=" + std::to_string(rows));
+            if (c < alpha) {
+                el.push_back(0);
+                es.push_back(-tmap[c] - 1);
+            } else {
+                el.push_back(lvl[c - alpha]);
+                es.push_back(slot[c - alpha]);
+            }
+            er.push_back(row);
+        }
+        finish_emissions(*p, el, es, er);
+        fill_common_stats(*p);
+        validate_plan(*p);
+        *out = p.release();
+    });
+}
+
+extern "C" int gmr_plan_from_layered(int rows, int cols, int alpha, int total_layered_rules,
+                                     const LayeredRule* rules, const int* val_indices,
+                                     const int* col_indices, const float* V, int n_vals,
+                                     const GPUSchedule* sched, gmr_plan** out) {
+    return guarded([&] {
+        if (!out || !sched || rows < 0 || cols < 1 || alpha < 1 || total_layered_rules < 0 || n_vals < 0)
+            throw Error(GMR_ERR_ARG, "bad argument");
+        if (total_layered_rules > 0 && !rules) throw Error(GMR_ERR_ARG, "null rules");
+        if (alpha > 1 && (!val_indices || !col_indices)) throw Error(GMR_ERR_ARG, "null terminal tables");
+        const int D = sched->max_depth;
+        if (D < 0 || (D > 0 && !sched->level_offsets)) throw Error(GMR_ERR_FORMAT, "bad schedule depth");
+        auto p = std::make_unique<gmr_plan>();
+        p->rows = rows;
+        p->cols = cols;
+        p->depth = D;
+        p->V.assign(V, V + n_vals);
+        for (int q = 1; q < alpha; ++q) {
+            p->term_val.push_back(val_indices[q - 1]);
+            p->term_col.push_back(col_indices[q - 1]);
+        }
+        const int* lo = sched->level_offsets;
+        if (D > 0 && (lo[0] != 0 || lo[D] != total_layered_rules))
+            throw Error(GMR_ERR_FORMAT, "level offsets do not cover the rules");
+        const int* eo = sched->emit_offsets;
+        if (sched->emit_total > 0 && (!eo || !sched->emit_pos || !sched->emit_row))
+            throw Error(GMR_ERR_FORMAT, "null emit lists");
+
+        std::vector<int32_t> el, es, er;
+        for (int e = 0; e < sched->num_term_emit; ++e) {
+            int s = sched->term_emit_sym[e];
+            if (s < 0 || s >= alpha) throw Error(GMR_ERR_FORMAT, "terminal emission symbol out of range");
+            el.push_back(0);
+            es.push_back(-s - 1);
+            er.push_back(sched->term_emit_row[e]);
+        }
+        p->lvl_off.assign(D + 1, 0);
+        std::vector<int32_t> prev, cur;  // frontier slot -> plan reference
+        bool coeff = false;
+        for (int64_t i = 0; i < total_layered_rules; ++i)
+            if (rules[i].coeff != 1.0f) coeff = true;
+        int64_t next = 0, identities = 0;
+        auto resolve = [&](int c, int k) -> int32_t {
+            if (c >= 0) {
+                if (c >= (int)prev.size())
+                    throw Error(GMR_ERR_FORMAT, "level " + std::to_string(k) + ": child slot " + std::to_string(c) +
+                                                    " beyond the previous frontier");
+                return prev[c];
+            }
+            if ((int64_t)(-(int64_t)c - 1) >= alpha) throw Error(GMR_ERR_FORMAT, "terminal child out of range");
+            return c;
+        };
+        for (int k = 1; k <= D; ++k) {
+            int a = lo[k - 1], b = lo[k];
+            if (b < a) throw Error(GMR_ERR_FORMAT, "level offsets decrease");
+            cur.assign((size_t)(b - a), 0);
+            std::vector<int32_t> L, Rr, idx;
+            std::vector<float> Cf;
+            for (int j = a; j < b; ++j) {
+                int32_t l = resolve(rules[j].left, k), r = resolve(rules[j].right, k);
+                float c = rules[j].coeff;
+                if (c == 1.0f && r == -1) {
+                    cur[j - a] = l;  // identity (pass-through): alias
+                    ++identities;
+                } else if (c == 1.0f && l == -1) {
+                    cur[j - a] = r;
+                    ++identities;
+                } else {
+                    L.push_back(l);
+                    Rr.push_back(r);
+                    Cf.push_back(c);
+                    idx.push_back(j - a);
+                }
+            }
+            auto perm = child_sort(L, Rr);
+            for (size_t q = 0; q < perm.size(); ++q) {
+                cur[idx[perm[q]]] = (int32_t)(next + (int64_t)q);
+                p->op_l.push_back(L[perm[q]]);
+                p->op_r.push_back(Rr[perm[q]]);
+                if (coeff) p->op_c.push_back(Cf[perm[q]]);
+            }
+            next += (int64_t)perm.size();
+            p->lvl_off[k] = next;
+            // emissions of level k
+            if (sched->emit_total > 0) {
+                for (int e = eo[k - 1]; e < eo[k]; ++e) {
+                    int pos = sched->emit_pos[e];
+                    if (pos < 0 || pos >= (int)cur.size()) throw Error(GMR_ERR_FORMAT, "emission position out of range");
+                    el.push_back(0);  // level of the source, fixed once all slots exist
+                    es.push_back(cur[pos]);
+                    er.push_back(sched->emit_row[e]);
+                }
+            }
+            prev.swap(cur);
+        }
+        // levels of emission sources (slots are final now)
+        for (size_t e = 0; e < es.size(); ++e) el[e] = es[e] < 0 ? 0 : level_of_slot(p->lvl_off, es[e]);
+        for (size_t e = 0; e < er.size(); ++e)
+            if (er[e] < 0 || er[e] >= rows) throw Error(GMR_ERR_FORMAT, "emission row out of range");
+        finish_emissions(*p, el, es, er);
+        fill_common_stats(*p);
+        auto& s = p->stats;
+        s.ref_layered = total_layered_rules;
+        s.ref_passthrough = identities;
+        s.ref_raw = total_layered_rules - identities;
+        s.ref_max_width = sched->max_width;
+        s.ref_emit = sched->emit_total;
+        s.ref_term_emit = sched->num_term_emit;
+        s.ref_alpha = alpha;
+        validate_plan(*p);
+        *out = p.release();
+    });
+}
+
+extern "C" int gmr_plan_get_stats(const gmr_plan* p, gmr_plan_stats* s) {
+    return guarded([&] {
+        if (!p || !s) throw Error(GMR_ERR_ARG, "null argument");
+        *s = p->stats;
+    });
+}
+
+extern "C" int gmr_plan_level_ops(const gmr_plan* p, int64_t* out, int n) {
+    return guarded([&] {
+        if (!p || !out || n < p->depth + 1) throw Error(GMR_ERR_ARG, "bad argument");
+        out[0] = 0;
+        for (int k = 1; k <= p->depth; ++k) out[k] = p->lvl_off[k] - p->lvl_off[k - 1];
+    });
+}
+
+extern "C" int gmr_plan_level_emits(const gmr_plan* p, int64_t* out, int n) {
+    return guarded([&] {
+        if (!p || !out || n < p->depth + 1) throw Error(GMR_ERR_ARG, "bad argument");
+        for (int k = 0; k <= p->depth; ++k) out[k] = p->em_off[k + 1] - p->em_off[k];
+    });
+}
+
+extern "C" double gmr_plan_alg_bytes(const gmr_plan* p, int semiring, int B) {
+    if (!p || B < 1) return -1.0;
+    const auto& s = p->stats;
+    double Bp = semiring == GMR_BOOLEAN ? (double)((B + 31) / 32) : (double)B;
+    return 12.0 * (double)s.ref_layered + 8.0 * (double)s.ref_emit + 8.0 * (double)s.ref_term_emit +
+           8.0 * (double)(s.ref_alpha - 1) + 4.0 * (double)s.n_vals + 4.0 * (double)s.cols * Bp +
+           4.0 * (double)s.rows * Bp;
+}
+
+extern "C" int gmr_plan_describe(const gmr_plan* p, char* buf, size_t cap) {
+    return guarded([&] {
+        if (!p || !buf || cap == 0) throw Error(GMR_ERR_ARG, "bad argument");
+        std::string o;
+        char line[256];
+        const auto& s = p->stats;
+        std::snprintf(line, sizeof line,
+                      "Max depth (L): %d, Max width (w*): %lld, Total layered rules: %lld (raw NTs: %lld, +pt: %lld), "
+                      "emissions: %lld+%lld term\n",
+                      p->depth, (long long)s.ref_max_width, (long long)s.ref_layered, (long long)s.ref_raw,
+                      (long long)s.ref_passthrough, (long long)s.ref_emit, (long long)s.ref_term_emit);
+        o += line;
+        std::snprintf(line, sizeof line, "Plan: ops=%lld (pass-throughs elided), terminals U=%lld, coeff=%d\n",
+                      (long long)s.n_ops, (long long)s.n_terms, s.has_coeff);
+        o += line;
+        o += "Level\tOps\tEmits\n";
+        std::snprintf(line, sizeof line, "0\t0\t%lld\n", (long long)(p->em_off[1] - p->em_off[0]));
+        o += line;
+        for (int k = 1; k <= p->depth; ++k) {
+            std::snprintf(line, sizeof line, "%d\t%lld\t%lld\n", k, (long long)(p->lvl_off[k] - p->lvl_off[k - 1]),
+                          (long long)(p->em_off[k + 1] - p->em_off[k]));
+            o += line;
+        }
+        std::snprintf(buf, cap, "%s", o.c_str());
+        if (o.size() + 1 > cap) throw Error(GMR_ERR_RANGE, "buffer too small: need " + std::to_string(o.size() + 1));
+    });
+}
+
+extern "C" int gmr_plan_array(const gmr_plan* p, int which, const void** ptr, int64_t* n) {
+    return guarded([&] {
+        if (!p || !ptr || !n) throw Error(GMR_ERR_ARG, "null argument");
+        switch (which) {
+            case 0: *ptr = p->op_l.data(); *n = (int64_t)p->op_l.size(); break;
+            case 1: *ptr = p->op_r.data(); *n = (int64_t)p->op_r.size(); break;
+            case 2: *ptr = p->op_c.data(); *n = (int64_t)p->op_c.size(); break;
+            case 3: *ptr = p->lvl_off.data(); *n = (int64_t)p->lvl_off.size(); break;
+            case 4: *ptr = p->em_off.data(); *n = (int64_t)p->em_off.size(); break;
+            case 5: *ptr = p->em_src.data(); *n = (int64_t)p->em_src.size(); break;
+            case 6: *ptr = p->em_row.data(); *n = (int64_t)p->em_row.size(); break;
+            case 7: *ptr = p->term_val.data(); *n = (int64_t)p->term_val.size(); break;
+            case 8: *ptr = p->term_col.data(); *n = (int64_t)p->term_col.size(); break;
+            case 9: *ptr = p->V.data(); *n = (int64_t)p->V.size(); break;
+            default: throw Error(GMR_ERR_ARG, "unknown plan array");
+        }
+    });
+}
+
+extern "C" void gmr_plan_free(gmr_plan* p) { delete p; }

@@ -1,0 +1,283 @@
+/*
+ * gmr.h -- C-ABI of the GB300-native engine for right multiplication
+ * y = M x and Y = M X over RePair grammar-compressed matrices.
+ *
+ * Two groups of entry points:
+ *
+ *  1. The drop-in legacy pair, with exactly the signatures of the
+ *     reference's gpu-engine/gpu_engine.h:239-276
+ *       run_gpu_right_multiply_layered   (replaces gpu_engine.cu:364-397)
+ *       run_gpu_right_multiply_batched   (replaces gpu_engine.cu:563-586)
+ *     They take the reference's proper-layered schedule (LayeredRule +
+ *     GPUSchedule, gpu-engine/layered_types.h:45-75) in HOST memory, choose
+ *     the semiring from the SEMIRING environment variable, run `iters`
+ *     multiplies and print the same stdout lines as the reference
+ *     ("GPU kernel: ... ms/vector.", "MEM analytic bytes: ...", ...).
+ *     Like the reference they return nothing; on a CUDA error they print
+ *     "CUDA Error: ..." and exit(1) (gpu_engine.cu:38-46).
+ *
+ *  2. A status-returning handle API (no counterpart function in the
+ *     reference; it splits the reference's per-call "allocate, copy,
+ *     sweep, copy back, free" into load-once / multiply-many):
+ *       grammar I/O   gmr_grammar_*   (.vc.R / .vc.C / .val, the format read
+ *                                      at gpu_engine_test.cu:291-345)
+ *       generators    gmr_gen_*, gmr_repair_compress (synthetic inputs)
+ *       schedule      gmr_plan_*      (replaces build_schedule.cpp:42-227 and
+ *                                      host_scheduler.cpp:31-102)
+ *       engine        gmr_engine_*    (device-resident multiply)
+ *     Every call returns GMR_OK (0) or an error code; gmr_last_error()
+ *     gives the message of the calling thread's last failure.
+ *
+ * No CUDA or torch types appear in the signatures: streams are passed as
+ * `void*` (a cudaStream_t), device buffers as plain pointers.
+ */
+#ifndef GMR_H
+#define GMR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+/* The reference's schedule structs, byte-identical to
+ * gpu-engine/layered_types.h:45-75 and guarded by the same macro, so a
+ * caller that already included the reference header keeps its definitions. */
+#ifndef LAYERED_TYPES_H
+#define LAYERED_TYPES_H
+struct LayeredRule {
+    int left;    /* >= 0: slot in the previous frontier; < 0: terminal T[-left-1] */
+    int right;   /* same encoding; -1 is the zero terminal T[0] */
+    float coeff; /* 1 for binary / pass-through rules, t for run-length rules */
+};
+struct GPUSchedule {
+    int max_depth;
+    int max_width;
+    int* level_offsets;  /* max_depth + 1 */
+    int* level_widths;   /* max_depth + 1 */
+    int* emit_offsets;   /* max_depth + 1 */
+    int* emit_pos;       /* emit_total */
+    int* emit_row;       /* emit_total */
+    int  emit_total;
+    int* term_emit_sym;  /* num_term_emit, index into T */
+    int* term_emit_row;  /* num_term_emit */
+    int  num_term_emit;
+};
+#endif
+#ifndef __cplusplus
+typedef struct LayeredRule LayeredRule;
+typedef struct GPUSchedule GPUSchedule;
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ */
+/* Status codes and semirings                                          */
+/* ------------------------------------------------------------------ */
+enum {
+    GMR_OK = 0,
+    GMR_ERR_ARG = 1,      /* bad argument (null pointer, negative size, ...) */
+    GMR_ERR_FORMAT = 2,   /* malformed grammar / schedule (out-of-range child, ...) */
+    GMR_ERR_IO = 3,       /* file could not be opened / read / written */
+    GMR_ERR_CUDA = 4,     /* a CUDA runtime call failed */
+    GMR_ERR_OOM = 5,      /* host or device allocation failed */
+    GMR_ERR_RANGE = 6,    /* size beyond a documented limit */
+    GMR_ERR_TIMEOUT = 7,  /* a bounded device-side wait gave up */
+    GMR_ERR_STATE = 8     /* object used in a state that does not allow it */
+};
+
+/* Semirings (gpu_engine.h:46-97).  Element types of X / Y:
+ *   GMR_PLUS_TIMES  float   X[cols][B], Y[rows][B]            (+, x)
+ *   GMR_BOOLEAN     uint32  X[cols][W], Y[rows][W], W=ceil(B/32):
+ *                           bit b%32 of word b/32 is right-hand side b  (OR, AND)
+ *   GMR_TROPICAL    int32   X[cols][B], Y[rows][B]            (min, +)
+ *                           inputs >= 1000000000 (INT_MAX included) are +inf;
+ *                           outputs use 1000000000 for +inf, as the reference.
+ * Right-hand sides are innermost ("column-contiguous"): X[j*B + b]. */
+enum { GMR_PLUS_TIMES = 0, GMR_BOOLEAN = 1, GMR_TROPICAL = 2 };
+
+#define GMR_TROPICAL_INF 1000000000
+
+const char* gmr_last_error(void);
+const char* gmr_version(void);
+
+/* ------------------------------------------------------------------ */
+/* Grammar (the mm-repair on-disk format)                              */
+/* ------------------------------------------------------------------ */
+typedef struct gmr_grammar gmr_grammar;
+typedef struct {
+    int alpha;          /* terminal / non-terminal boundary */
+    int64_t n_rules;
+    int64_t c_len;      /* length of the top sequence C (0 = row end) */
+    int n_vals;         /* distinct values (.val) */
+    int has_runlen;     /* 1 if any rule is run-length */
+} gmr_grammar_info;
+
+/* Reads <base>.vc.R (int32 alpha, then int32 (left,right) pairs),
+ * <base>.vc.C (int32 top sequence) and <base>.val (float64 values). */
+int gmr_grammar_load(const char* base, gmr_grammar** out);
+int gmr_grammar_save(const gmr_grammar* g, const char* base);
+/* rules: 2*n_rules ints (left, right).  kinds/reps may be NULL (all binary);
+ * kind 1 = run-length N -> left^rep (grammar.h:43-48). */
+int gmr_grammar_create(int alpha, int64_t n_rules, const int32_t* rules,
+                       const int32_t* kinds, const int32_t* reps,
+                       int64_t c_len, const int32_t* C,
+                       int n_vals, const double* V, gmr_grammar** out);
+int gmr_grammar_get_info(const gmr_grammar* g, gmr_grammar_info* info);
+const int32_t* gmr_grammar_rules(const gmr_grammar* g);  /* 2*n_rules */
+const int32_t* gmr_grammar_kinds(const gmr_grammar* g);  /* n_rules */
+const int32_t* gmr_grammar_reps(const gmr_grammar* g);   /* n_rules */
+const int32_t* gmr_grammar_C(const gmr_grammar* g);      /* c_len */
+const double*  gmr_grammar_V(const gmr_grammar* g);      /* n_vals */
+void gmr_grammar_free(gmr_grammar* g);
+
+/* ------------------------------------------------------------------ */
+/* Uncompressed CSRV matrices, seeded generators, RePair                */
+/* ------------------------------------------------------------------ */
+/* A CSRV string: per row the terminal codes val_idx*cols + col + 1 in
+ * increasing column order, then 0.  (The format mm-repair compresses.) */
+typedef struct gmr_csrv gmr_csrv;
+typedef struct {
+    int rows, cols;
+    int64_t len;   /* codes including the row delimiters */
+    int64_t nnz;
+    int n_vals;
+} gmr_csrv_info;
+
+int gmr_csrv_create(int rows, int cols, int64_t len, const int32_t* codes,
+                    int n_vals, const double* V, gmr_csrv** out);
+/* Dense row-major matrix -> CSRV; distinct non-zero values sorted ascending. */
+int gmr_csrv_from_dense(int rows, int cols, const double* M, gmr_csrv** out);
+int gmr_csrv_get_info(const gmr_csrv* m, gmr_csrv_info* info);
+const int32_t* gmr_csrv_codes(const gmr_csrv* m);
+const double*  gmr_csrv_V(const gmr_csrv* m);
+void gmr_csrv_free(gmr_csrv* m);
+
+/* Genotype-like mosaic: rows = sites, cols = haplotypes, value 1. */
+int gmr_gen_mosaic(int rows, int cols, int founders, double switch_rate,
+                   double mutation, uint64_t seed, int n_threads, gmr_csrv** out);
+/* Copy-model directed graph, row = node.  weighted = 0: value 1;
+ * weighted = 1: integer weights 1..100 (copied entries keep their weight). */
+int gmr_gen_copy_graph(int nodes, int degree, double copy_prob, int weighted,
+                       uint64_t seed, int n_threads, gmr_csrv** out);
+/* Grammar compression of a CSRV string by rounds of RePair pair
+ * replacement (most frequent pairs first; rules never span a row end). */
+int gmr_repair_compress(const gmr_csrv* m, int n_threads, gmr_grammar** out);
+
+/* ------------------------------------------------------------------ */
+/* Schedule ("plan"): level-major, child-sorted layout                 */
+/* ------------------------------------------------------------------ */
+typedef struct gmr_plan gmr_plan;
+typedef struct {
+    int rows, cols, depth, n_vals, has_coeff;
+    int64_t n_ops;        /* evaluated rules (identity pass-throughs elided) */
+    int64_t n_emit;       /* non-terminal emissions */
+    int64_t n_term_emit;  /* terminal emissions */
+    int64_t n_terms;      /* compacted terminals U, zero terminal included */
+    int64_t max_level_ops;
+    /* The reference's proper-layered figures for the same grammar
+     * (build_schedule.cpp:42-227): L = depth, w*, |R|, +pt, emissions, U. */
+    int64_t ref_layered, ref_raw, ref_passthrough;
+    int64_t ref_max_width, ref_emit, ref_term_emit, ref_alpha;
+} gmr_plan_stats;
+
+int gmr_plan_build(const gmr_grammar* g, int rows, int cols, gmr_plan** out);
+int gmr_plan_from_layered(int rows, int cols, int alpha, int total_layered_rules,
+                          const LayeredRule* rules, const int* val_indices,
+                          const int* col_indices, const float* V, int n_vals,
+                          const GPUSchedule* sched, gmr_plan** out);
+int gmr_plan_get_stats(const gmr_plan* p, gmr_plan_stats* s);
+/* ops[k] for k = 0..depth (ops[0] = 0) */
+int gmr_plan_level_ops(const gmr_plan* p, int64_t* out, int n);
+/* emissions of level k (k = 0: terminal emissions) for k = 0..depth */
+int gmr_plan_level_emits(const gmr_plan* p, int64_t* out, int n);
+/* Algorithmic bytes of one multiply of B right-hand sides, the reference's
+ * analytic accounting (gpu_engine.cu:174-184) without the scratch frontiers:
+ * 12*N_L + 8*E + 8*E_T + 8*(U-1) + 4*n_V + 4*cols*B' + 4*rows*B',
+ * B' = B, or ceil(B/32) for the bit-packed Boolean semiring. */
+double gmr_plan_alg_bytes(const gmr_plan* p, int semiring, int B);
+/* Read-only view of a plan array, for inspection and tests:
+ * which = 0 op_l, 1 op_r (int32 references: >= 0 arena slot, < 0 terminal
+ * -ref-1), 2 op_c (float, absent unless run-length rules exist), 3 lvl_off
+ * (int64, depth+1), 4 em_off (int64, depth+2), 5 em_src (int32),
+ * 6 em_row (int32), 7 term_val (int32), 8 term_col (int32), 9 V (float).
+ * *ptr stays valid until gmr_plan_free. */
+int gmr_plan_array(const gmr_plan* p, int which, const void** ptr, int64_t* n);
+/* Human-readable per-level report (the host_scheduler inspector). */
+int gmr_plan_describe(const gmr_plan* p, char* buf, size_t cap);
+void gmr_plan_free(gmr_plan* p);
+
+/* ------------------------------------------------------------------ */
+/* Engine: device-resident schedule + multiply                          */
+/* ------------------------------------------------------------------ */
+typedef struct gmr_engine gmr_engine;
+
+/* Kernel-variant knobs; 0 = let the engine choose. */
+typedef struct {
+    int variant;      /* GMR_VARIANT_* */
+    int vec_tile;     /* right-hand sides per sweep tile (0 = all B) */
+    int ops_per_cta;  /* work items per CTA hint */
+    int emit_mode;    /* GMR_EMIT_* */
+} gmr_config;
+enum {
+    GMR_VARIANT_AUTO = 0,
+    GMR_VARIANT_PLAIN = 1,   /* per-level launches, one atomic per emission */
+    GMR_VARIANT_FUSED = 2,   /* per-level launches, ops+emits fused, segmented emits */
+    GMR_VARIANT_GRAPH = 3,   /* FUSED captured once into a CUDA graph */
+    GMR_VARIANT_PERSISTENT = 4 /* one cooperative launch walks every level */
+};
+enum { GMR_EMIT_AUTO = 0, GMR_EMIT_ATOMIC = 1, GMR_EMIT_SEGMENTED = 2 };
+
+int gmr_engine_create(const gmr_plan* p, int device, gmr_engine** out);
+/* dX, dY: device pointers (layouts above). stream: cudaStream_t or NULL. */
+int gmr_engine_multiply(gmr_engine* e, int semiring, const void* dX, void* dY,
+                        int B, const gmr_config* cfg, void* stream);
+/* Host buffers: copies X in, multiplies, copies Y out, synchronous. */
+int gmr_engine_multiply_host(gmr_engine* e, int semiring, const void* hX,
+                             void* hY, int B, const gmr_config* cfg);
+/* Runs one multiply launch by launch (no graph) with a CUDA event pair
+ * around every launch and writes the device time of each launch (ms) to
+ * ms[0..*n): launch 0 is the prologue (Y = zero, terminal values), launch k
+ * evaluates level k and folds the emissions of level k-1, the last launch
+ * folds the emissions of the top level.  The engine's timing recorder. */
+int gmr_engine_time_launches(gmr_engine* e, int semiring, const void* dX, void* dY,
+                             int B, const gmr_config* cfg, void* stream,
+                             float* ms, int cap, int* n);
+/* Kernel launches issued by the calling thread's last multiply. */
+int64_t gmr_engine_last_launches(const gmr_engine* e);
+/* Device bytes held by the engine (schedule + scratch). */
+int64_t gmr_engine_device_bytes(const gmr_engine* e);
+void gmr_engine_free(gmr_engine* e);
+
+/* ------------------------------------------------------------------ */
+/* Drop-in legacy entry points (gpu_engine.h:239-276)                   */
+/* ------------------------------------------------------------------ */
+#ifdef __cplusplus
+void run_gpu_right_multiply_layered(
+    int rows, int cols, int alpha, int total_layered_rules,
+    const LayeredRule* h_rules, const int* h_val_indices, const int* h_col_indices,
+    const float* h_V, int num_distinct_vals, const float* h_x,
+    const GPUSchedule& h_sched, float* h_y, int iters);
+void run_gpu_right_multiply_batched(
+    int rows, int cols, int alpha, int total_layered_rules,
+    const LayeredRule* h_rules, const int* h_val_indices, const int* h_col_indices,
+    const float* h_V, int num_distinct_vals, const float* h_X,
+    const GPUSchedule& h_sched, float* h_Y, int B, int iters);
+#else
+/* C view: the C++ reference parameter is passed as a pointer. */
+void run_gpu_right_multiply_layered(
+    int rows, int cols, int alpha, int total_layered_rules,
+    const LayeredRule* h_rules, const int* h_val_indices, const int* h_col_indices,
+    const float* h_V, int num_distinct_vals, const float* h_x,
+    const GPUSchedule* h_sched, float* h_y, int iters);
+void run_gpu_right_multiply_batched(
+    int rows, int cols, int alpha, int total_layered_rules,
+    const LayeredRule* h_rules, const int* h_val_indices, const int* h_col_indices,
+    const float* h_V, int num_distinct_vals, const float* h_X,
+    const GPUSchedule* h_sched, float* h_Y, int B, int iters);
+#endif
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GMR_H */

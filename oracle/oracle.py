@@ -1,0 +1,165 @@
+"""ctypes wrapper of the oracle (oracle.c) -- TEST INFRASTRUCTURE ONLY.
+
+Imported by tests/, by the smoke check in __graft_entry__.py and by the CPU
+baseline leg of bench.py, as the checker (and as the timed CPU baseline).  The
+product path (g-mm-repair_gb300/gmr) never imports it.  Each function names the
+reference code it restates (see oracle.c).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+PLUS, BOOL, TROP = 0, 1, 2
+NAMES = {0: "plustimes", 1: "boolean", 2: "tropical"}
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    src = HERE / "oracle.c"
+    if force or not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
+        subprocess.run(["make", "-s", "-C", str(HERE), "-B", "liboracle.so"], check=True)
+    return LIB
+
+
+def build_ref() -> bool:
+    """Builds the reference's own sources into oracle/_ref (only where the
+    reference tree exists)."""
+    if not Path("/root/reference/gpu-engine").is_dir():
+        return False
+    r = subprocess.run(["make", "-s", "-C", str(HERE), "ref"], capture_output=True, text=True)
+    return r.returncode == 0
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        l = C.CDLL(str(LIB))
+        P, I = C.c_void_p, C.POINTER(C.c_int)
+        l.orc_build_schedule.argtypes = [C.c_int, C.c_long, I, I, I, C.c_long, I, C.POINTER(P)]
+        l.orc_sched_free.argtypes = [P]
+        l.orc_sched_int.argtypes = [P, C.c_int, C.POINTER(C.c_long)]
+        l.orc_sched_arr.argtypes = [P, C.c_int]
+        l.orc_sched_arr.restype = I
+        l.orc_sched_coeff.argtypes = [P]
+        l.orc_sched_coeff.restype = C.POINTER(C.c_float)
+        l.orc_sweep_f64.argtypes = [P, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_float), C.c_int, C.c_int,
+                                    C.POINTER(C.c_double)]
+        l.orc_cpu_reference.argtypes = [P, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.c_int,
+                                        P, C.c_int]
+        l.orc_expand.argtypes = [C.c_int, C.c_long, I, I, I, C.c_long, I, I]
+        l.orc_expand.restype = C.c_long
+        l.orc_brute_force.argtypes = [C.c_long, I, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_float), C.c_int,
+                                      C.c_int, C.POINTER(C.c_double)]
+        _lib = l
+    return _lib
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int)) if a is not None else None
+
+
+class RefSchedule:
+    """The reference's BuiltSchedule (build_schedule.cpp:42-227), restated."""
+
+    INTS = ["alpha", "depth", "max_width", "num_raw", "num_layered", "num_pt", "emit_total", "num_term"]
+
+    def __init__(self, alpha, rules, C_seq, kinds=None, reps=None):
+        rules = np.ascontiguousarray(np.asarray(rules, dtype=np.int32).reshape(-1))
+        C_seq = np.ascontiguousarray(C_seq, dtype=np.int32)
+        kinds = None if kinds is None else np.ascontiguousarray(kinds, dtype=np.int32)
+        reps = None if reps is None else np.ascontiguousarray(reps, dtype=np.int32)
+        h = C.c_void_p()
+        lib().orc_build_schedule(int(alpha), len(rules) // 2, _ip(rules), _ip(kinds), _ip(reps), len(C_seq),
+                                 _ip(C_seq), C.byref(h))
+        self._h = h
+        v = C.c_long()
+        for i, n in enumerate(self.INTS):
+            lib().orc_sched_int(h, i, C.byref(v))
+            setattr(self, n, int(v.value))
+        L, D = self.num_layered, self.depth
+
+        def arr(which, n):
+            if n == 0:
+                return np.zeros(0, np.int32)
+            return np.ctypeslib.as_array(lib().orc_sched_arr(h, which), shape=(n,)).copy()
+
+        self.left, self.right = arr(0, L), arr(1, L)
+        self.coeff = (np.ctypeslib.as_array(lib().orc_sched_coeff(h), shape=(L,)).copy() if L
+                      else np.zeros(0, np.float32))
+        self.level_offsets, self.level_widths = arr(2, D + 1), arr(3, D + 1)
+        self.emit_offsets = arr(4, D + 1)
+        self.emit_pos, self.emit_row = arr(5, self.emit_total), arr(6, self.emit_total)
+        self.term_emit_sym, self.term_emit_row = arr(7, self.num_term), arr(8, self.num_term)
+        self.term_orig = arr(9, self.alpha)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().orc_sched_free(self._h)
+            self._h = C.c_void_p()
+
+    def rules_lrc(self):
+        out = np.zeros(self.num_layered, dtype=[("l", "<i4"), ("r", "<i4"), ("c", "<f4")])
+        out["l"], out["r"], out["c"] = self.left, self.right, self.coeff
+        return out
+
+    def gpu_schedule(self) -> dict:
+        return dict(max_depth=self.depth, max_width=self.max_width, level_offsets=self.level_offsets,
+                    level_widths=self.level_widths, emit_offsets=self.emit_offsets, emit_pos=self.emit_pos,
+                    emit_row=self.emit_row, term_emit_sym=self.term_emit_sym, term_emit_row=self.term_emit_row)
+
+    def terminal_tables(self, cols):
+        """val/col index tables as gpu_engine_test.cu:373-380 builds them."""
+        t = self.term_orig[1:].astype(np.int64)
+        return ((t - 1) // cols).astype(np.int32), ((t - 1) % cols).astype(np.int32)
+
+    def sweep_f64(self, semiring, V, x, rows, cols) -> np.ndarray:
+        V = np.ascontiguousarray(V, dtype=np.float64)
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.zeros(rows, dtype=np.float64)
+        lib().orc_sweep_f64(self._h, semiring, V.ctypes.data_as(C.POINTER(C.c_double)),
+                            x.ctypes.data_as(C.POINTER(C.c_float)), rows, cols,
+                            y.ctypes.data_as(C.POINTER(C.c_double)))
+        return y
+
+    def cpu_reference(self, semiring, V, x, rows, cols, threads=1) -> np.ndarray:
+        Vf = np.ascontiguousarray(V, dtype=np.float32)
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.zeros(rows, dtype=np.float32 if semiring == PLUS else np.int32)
+        lib().orc_cpu_reference(self._h, semiring, Vf.ctypes.data_as(C.POINTER(C.c_float)),
+                                x.ctypes.data_as(C.POINTER(C.c_float)), rows, cols,
+                                y.ctypes.data_as(C.c_void_p), threads)
+        return y
+
+
+def expand(alpha, rules, C_seq, kinds=None, reps=None) -> np.ndarray:
+    """CSRV string re-expanded from a grammar (cpu_selftest.cpp:119-156)."""
+    rules = np.ascontiguousarray(np.asarray(rules, dtype=np.int32).reshape(-1))
+    C_seq = np.ascontiguousarray(C_seq, dtype=np.int32)
+    kinds = None if kinds is None else np.ascontiguousarray(kinds, dtype=np.int32)
+    reps = None if reps is None else np.ascontiguousarray(reps, dtype=np.int32)
+    n = lib().orc_expand(int(alpha), len(rules) // 2, _ip(rules), _ip(kinds), _ip(reps), len(C_seq), _ip(C_seq),
+                         None)
+    out = np.zeros(max(n, 1), dtype=np.int32)
+    lib().orc_expand(int(alpha), len(rules) // 2, _ip(rules), _ip(kinds), _ip(reps), len(C_seq), _ip(C_seq),
+                     _ip(out))
+    return out[:n]
+
+
+def brute_force(vc, semiring, V, x, rows, cols) -> np.ndarray:
+    """y = M x straight from the CSRV string (cpu_selftest.cpp:104-117)."""
+    vc = np.ascontiguousarray(vc, dtype=np.int32)
+    V = np.ascontiguousarray(V, dtype=np.float64)
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.zeros(rows, dtype=np.float64)
+    lib().orc_brute_force(len(vc), _ip(vc), semiring, V.ctypes.data_as(C.POINTER(C.c_double)),
+                          x.ctypes.data_as(C.POINTER(C.c_float)), rows, cols,
+                          y.ctypes.data_as(C.POINTER(C.c_double)))
+    return y

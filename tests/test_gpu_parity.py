@@ -1,0 +1,251 @@
+"""CUDA engine (libgmr.so, through the C-ABI) against the oracle.
+
+Tolerances: (+,x) fp32 results are compared with an FP64 oracle sweep on
+float32-rounded values V, as relative max-norm ||y - y64||_inf / ||y64||_inf
+<= 1e-5; (OR,AND) and (min,+) results must be bit-exact against the oracle's
+restatement of the reference's int sweep (gpu_engine_test.cu:49-104)."""
+import os
+
+import numpy as np
+import pytest
+
+import gmr
+from helpers import INF, SEMIRINGS, golden_cases, golden_meta, load_case
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+VARIANTS = {"plain": gmr.VARIANT_PLAIN, "fused": gmr.VARIANT_FUSED, "graph": gmr.VARIANT_GRAPH}
+
+
+def relmax(y, ref):
+    ref = np.asarray(ref, dtype=np.float64)
+    den = max(np.abs(ref).max(initial=0.0), 1e-30)
+    return float(np.abs(np.asarray(y, dtype=np.float64) - ref).max(initial=0.0) / den)
+
+
+def random_X(sr, cols, B, seed):
+    rng = np.random.default_rng(seed)
+    if sr == 0:
+        return rng.uniform(-1, 1, (cols, B)).astype(np.float32)
+    if sr == 1:
+        return (rng.random((cols, B)) < 0.3).astype(np.float32)
+    X = rng.integers(0, 1000, (cols, B)).astype(np.float32)
+    X[rng.random((cols, B)) < 0.2] = 1e9
+    return X
+
+
+def engine_inputs(sr, X):
+    """float host matrix -> the engine's input words."""
+    if sr == 0:
+        return X.astype(np.float32)
+    if sr == 1:
+        return gmr.pack_bits(X)
+    return np.where(X >= INF, np.int32(2**31 - 1), X).astype(np.int32)  # INT_MAX = +inf
+
+
+def engine_outputs(sr, Y, B):
+    return gmr.unpack_bits(Y, B) if sr == 1 else Y
+
+
+def oracle_columns(sched, sr, V, X, rows, cols):
+    out = []
+    for b in range(X.shape[1]):
+        if sr == 0:
+            out.append(sched.sweep_f64(0, V.astype(np.float32).astype(np.float64), X[:, b], rows, cols))
+        else:
+            out.append(sched.cpu_reference(sr, V.astype(np.float32), X[:, b], rows, cols, threads=1))
+    return np.stack(out, axis=1)
+
+
+def check(sr, Y, ref):
+    if sr == 0:
+        assert relmax(Y, ref) <= TOL, relmax(Y, ref)
+    else:
+        np.testing.assert_array_equal(np.asarray(Y, dtype=np.int64), np.asarray(ref, dtype=np.int64))
+
+
+@pytest.fixture(params=golden_cases())
+def case(request):
+    c = load_case(request.param)
+    g = gmr.Grammar.from_arrays(int(c["alpha"]), c["rules"], c["C"], c["V"])
+    c["plan"] = gmr.Plan.build(g, int(c["rows"]), int(c["cols"]))
+    c["sched"] = O.RefSchedule(int(c["alpha"]), c["rules"], c["C"])
+    return c
+
+
+@pytest.mark.parametrize("sr", range(3))
+@pytest.mark.parametrize("variant", list(VARIANTS))
+def test_golden_single_vector(case, sr, variant):
+    """B = 1 against the reference's own stored outputs."""
+    name = SEMIRINGS[sr]
+    eng = gmr.Engine(case["plan"])
+    x = case[f"x_{name}"].reshape(-1, 1)
+    Y = engine_outputs(sr, eng.multiply(engine_inputs(sr, x), sr, B=1, variant=VARIANTS[variant]), 1)[:, 0]
+    if sr == 0:
+        ref = case["sched"].sweep_f64(0, case["V"].astype(np.float32).astype(np.float64), x[:, 0],
+                                      int(case["rows"]), int(case["cols"]))
+        check(0, Y, ref)
+        assert relmax(Y, case["y64_plustimes"]) <= 1e-5
+    else:
+        check(sr, Y, case[f"y32_{name}"])  # the reference's int sweep, bit for bit
+    assert eng.last_launches > 0
+
+
+@pytest.mark.parametrize("sr", range(3))
+@pytest.mark.parametrize("B", [2, 3, 8, 32, 33, 64, 128])
+def test_golden_batched(case, sr, B):
+    rows, cols = int(case["rows"]), int(case["cols"])
+    X = random_X(sr, cols, B, 100 + B)
+    ref = oracle_columns(case["sched"], sr, case["V"], X, rows, cols)
+    eng = gmr.Engine(case["plan"])
+    for variant in (gmr.VARIANT_PLAIN, gmr.VARIANT_GRAPH):
+        Y = engine_outputs(sr, eng.multiply(engine_inputs(sr, X), sr, B=B, variant=variant), B)
+        check(sr, Y, ref)
+
+
+@pytest.mark.parametrize("sr", range(3))
+def test_device_pointers_and_stream(case, sr):
+    torch = pytest.importorskip("torch")
+    rows, cols, B = int(case["rows"]), int(case["cols"]), 8
+    X = random_X(sr, cols, B, 7)
+    ref = oracle_columns(case["sched"], sr, case["V"], X, rows, cols)
+    Xw = engine_inputs(sr, X)
+    dX = torch.from_numpy(Xw.view(np.int32)).cuda()
+    dY = torch.empty((rows, Xw.shape[1]), dtype=torch.int32, device="cuda")
+    eng = gmr.Engine(case["plan"])
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        for _ in range(3):  # graph replay on a side stream
+            eng.multiply_device(sr, dX.data_ptr(), dY.data_ptr(), B, stream=s.cuda_stream)
+    s.synchronize()
+    Yw = dY.cpu().numpy().view({0: np.float32, 1: np.uint32, 2: np.int32}[sr])
+    check(sr, engine_outputs(sr, Yw, B), ref)
+
+
+@pytest.mark.parametrize("sr", range(3))
+def test_legacy_entry_points(case, sr, monkeypatch, capfd):
+    """The drop-in pair with the reference's layered schedule and stdout lines."""
+    name = SEMIRINGS[sr]
+    monkeypatch.setenv("SEMIRING", name)
+    s = case["sched"]
+    rows, cols = int(case["rows"]), int(case["cols"])
+    vi, ci = s.terminal_tables(cols)
+    Vf = case["V"].astype(np.float32)
+    x = case[f"x_{name}"]
+    y = gmr.run_gpu_right_multiply_layered(rows, cols, s.alpha, s.rules_lrc(), vi, ci, Vf, x, s.gpu_schedule(),
+                                           iters=3)
+    out = capfd.readouterr().out
+    assert "GPU kernel: " in out and " ms/vector." in out and "MEM analytic bytes: " in out
+    ref = case[f"y32_{name}"]
+    check(sr, y, ref if sr else case["sched"].sweep_f64(0, Vf.astype(np.float64), x, rows, cols))
+    B = 5
+    X = random_X(sr, cols, B, 3)
+    Y = gmr.run_gpu_right_multiply_batched(rows, cols, s.alpha, s.rules_lrc(), vi, ci, Vf, X.reshape(-1),
+                                           s.gpu_schedule(), B, iters=2)
+    assert "GPU batched (B=5): " in capfd.readouterr().out
+    check(sr, Y, oracle_columns(s, sr, case["V"], X, rows, cols))
+
+
+def test_unittest_grammar_runlength():
+    """cpu_selftest.cpp:374-467 grammar (run-length rule, coefficient 3)."""
+    g = gmr.Grammar.from_arrays(5, [[1, 2], [3, 5], [6, 0], [7, 5]], [8, 0], [1.5, 2.5], kinds=[0, 0, 1, 0],
+                                reps=[1, 1, 3, 1])
+    eng = gmr.Engine(gmr.Plan.build(g, 2, 3))
+    y = eng.multiply(np.array([0.5, -0.5, 1.0], np.float32), 0)[:, 0]
+    np.testing.assert_allclose(y, golden_meta()["unittest"]["y_sweep"], atol=1e-6)
+    Y = eng.multiply(np.tile(np.array([[0.5], [-0.5], [1.0]], np.float32), (1, 4)), 0)
+    np.testing.assert_allclose(Y, [[4.5] * 4, [0.0] * 4], atol=1e-6)
+
+
+def test_readme_worked_example():
+    c = load_case("readme_8x7")
+    g = gmr.Grammar.from_arrays(int(c["alpha"]), c["rules"], c["C"], c["V"])
+    eng = gmr.Engine(gmr.Plan.build(g, 8, 7))
+    y = eng.multiply(np.array(golden_meta()["readme"]["x"], np.float32), 0)[:, 0]
+    np.testing.assert_allclose(y, golden_meta()["readme"]["y"], rtol=1e-6)
+
+
+def test_terminals_only_and_empty_rows():
+    g = gmr.Grammar.from_arrays(4, np.zeros((0, 2), np.int32), [1, 3, 0, 0, 2, 0], [1.0])
+    eng = gmr.Engine(gmr.Plan.build(g, 4, 3))
+    y = eng.multiply(np.array([1.0, 2.0, 4.0], np.float32), 0)[:, 0]
+    np.testing.assert_allclose(y, [5.0, 0.0, 2.0, 0.0])
+    yt = eng.multiply(np.array([[5], [2**31 - 1], [7]], np.int32), 2)[:, 0]
+    np.testing.assert_array_equal(yt, [6, INF, INF, INF])
+
+
+def test_tropical_int_max_is_infinity():
+    # row 0: x0 + 1 and x1 + 1 (value 1) ; x1 = INT_MAX -> only x0 counts
+    g = gmr.Grammar.from_arrays(3, [[1, 2]], [3, 0, 2, 0], [1.0])
+    eng = gmr.Engine(gmr.Plan.build(g, 3, 2))
+    y = eng.multiply(np.array([[10], [2**31 - 1]], np.int32), 2)[:, 0]
+    np.testing.assert_array_equal(y, [11, INF, INF])
+
+
+def test_deterministic_boolean_tropical(case):
+    rows, cols, B = int(case["rows"]), int(case["cols"]), 64
+    eng = gmr.Engine(case["plan"])
+    for sr in (1, 2):
+        Xw = engine_inputs(sr, random_X(sr, cols, B, 9))
+        a = eng.multiply(Xw, sr, B=B)
+        b = eng.multiply(Xw, sr, B=B)
+        np.testing.assert_array_equal(a, b)
+
+
+# ---------------------------------------------------------------- C1 at full size
+@pytest.fixture(scope="module")
+def c1():
+    """Config 1: 20,000 x 5,000 mosaic, 64 founders, seed 0."""
+    m = gmr.gen_mosaic(20000, 5000, 64, 0.01, 1e-3, 0)
+    g = gmr.repair(m)
+    plan = gmr.Plan.build(g, 20000, 5000)
+    sched = O.RefSchedule(g.alpha, g.rules(), g.C())
+    return dict(g=g, plan=plan, sched=sched, V=g.values(), eng=gmr.Engine(plan))
+
+
+def test_c1_plain_spmv_vs_fp64(c1):
+    rng = np.random.default_rng(1)
+    x = rng.uniform(-1, 1, 5000).astype(np.float32)
+    ref = c1["sched"].sweep_f64(0, c1["V"], x, 20000, 5000)
+    for variant in VARIANTS.values():
+        y = c1["eng"].multiply(x, 0, variant=variant)[:, 0]
+        err = relmax(y, ref)
+        print(f"C1 B=1 variant={variant} rel max-norm error vs FP64 = {err:.3e}")
+        assert err <= TOL
+
+
+@pytest.mark.parametrize("B", [8, 32])
+def test_c1_batched_vs_fp64(c1, B):
+    rng = np.random.default_rng(B)
+    X = rng.uniform(-1, 1, (5000, B)).astype(np.float32)
+    Y = c1["eng"].multiply(X, 0, B=B)
+    for b in range(0, B, max(1, B // 4)):
+        ref = c1["sched"].sweep_f64(0, c1["V"], X[:, b], 20000, 5000)
+        assert relmax(Y[:, b], ref) <= TOL
+
+
+def test_c1_properties(c1):
+    """Size-independent checks at full size: linearity, OR- and min-homomorphism."""
+    eng, rng = c1["eng"], np.random.default_rng(5)
+    x1, x2 = rng.uniform(-1, 1, (2, 5000)).astype(np.float32)
+    y1, y2 = eng.multiply(x1, 0)[:, 0], eng.multiply(x2, 0)[:, 0]
+    y12 = eng.multiply((2 * x1 - 3 * x2).astype(np.float32), 0)[:, 0]
+    assert relmax(y12, 2 * y1.astype(np.float64) - 3 * y2) < 1e-5
+    b1, b2 = (rng.random((2, 5000, 64)) < 0.01)
+    Y1, Y2 = eng.multiply(gmr.pack_bits(b1), 1, B=64), eng.multiply(gmr.pack_bits(b2), 1, B=64)
+    np.testing.assert_array_equal(eng.multiply(gmr.pack_bits(b1 | b2), 1, B=64), Y1 | Y2)
+    t1 = rng.integers(0, 1000, (5000, 4)).astype(np.int32)
+    t2 = rng.integers(0, 1000, (5000, 4)).astype(np.int32)
+    T1, T2 = eng.multiply(t1, 2), eng.multiply(t2, 2)
+    np.testing.assert_array_equal(eng.multiply(np.minimum(t1, t2), 2), np.minimum(T1, T2))
+
+
+def test_c1_boolean_tropical_bit_exact(c1):
+    rng = np.random.default_rng(11)
+    for sr, B in ((1, 40), (2, 6)):
+        X = random_X(sr, 5000, B, 12)
+        Y = engine_outputs(sr, c1["eng"].multiply(engine_inputs(sr, X), sr, B=B), B)
+        for b in rng.choice(B, 4, replace=False):
+            ref = c1["sched"].cpu_reference(sr, c1["V"].astype(np.float32), X[:, b], 20000, 5000, threads=1)
+            np.testing.assert_array_equal(Y[:, b], ref)
