@@ -204,6 +204,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-seconds", type=float, default=6.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--dump-launches", action="store_true", help="per-launch times and level sizes to stderr")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -277,6 +278,13 @@ def main():
     lt = np.mean([eng.time_launches(0, X.data_ptr(), Y.data_ptr(), B, stream=sp, variant=2)
                   for _ in range(reps)], axis=0)
     level_ms = float(lt[1:].sum())       # k_level launches: levels + final fold
+    if args.dump_launches:
+        ops, ems = plan.level_ops(), plan.level_emits()
+        log("launch\tms\tops(level k)\temits(level k-1)")
+        for i, t_ms in enumerate(lt):
+            o = int(ops[i]) if 1 <= i < len(ops) else 0
+            em = int(ems[i - 1]) if 1 <= i <= len(ems) else 0
+            log(f"{i}\t{t_ms:.4f}\t{o}\t{em}")
     alg_total = plan.alg_bytes(0, B)
     alg_pro = 8.0 * (st["ref_alpha"] - 1) + 4.0 * st["n_vals"] + 4.0 * cols * B + 4.0 * rows * B
     alg_level = alg_total - alg_pro      # 12 N_L + 8 E + 8 E_T

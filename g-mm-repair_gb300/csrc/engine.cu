@@ -138,192 +138,316 @@ __device__ __forceinline__ void vred(typename S::T* p, const Vec<typename S::T, 
 }
 
 // ------------------------------------------------------------------ kernels
-struct LevelArgs {
-    // ops of this level
-    const int32_t* op_l;
-    const int32_t* op_r;
-    const float* op_c;  // nullptr: all coefficients are 1
-    int64_t op_first;   // first arena slot of the level
-    int64_t n_ops;
-    // emissions folded by this launch
-    const int32_t* em_src;
-    const int32_t* em_row;
-    int64_t em_first;
-    int64_t n_em;
-    int em_blocks;      // blocks [0, em_blocks) fold emissions, the rest evaluate ops
-    int em_chunk;       // emissions per lane group (segmented mode, G > 1)
-};
-
+// Work decomposition: a launch covers right-hand-side tiles
+// [t0, t0 + gridDim.y) of Bt words each (blockIdx.y = tile).  Within a tile an
+// item is (unit, lane): G = Bt / VEC lanes per unit (rule, emission or row
+// segment), each lane moving VEC consecutive words.  G is a power of two
+// given as GLOG (shifts, no division); GLOG < 0 selects a generic G.
+// The arena and the terminal table are tile-major ([tile][slot][Bt]) so the
+// values of one tile are dense; X and Y keep the caller's [row][Bw] layout.
 struct SweepArgs {
-    void* arena;   // [n_ops][Bw]
-    void* T;       // [U][Bw]
-    void* Y;       // [rows][Bw]
-    const void* X; // [cols][Bw]
+    void* arena;   // [ntile][n_ops][Bt]
+    void* T;       // [ntile][U][Bt]
+    void* Y;       // [rows][ldy]
+    const void* X; // [cols][ldx]
     const float* V;
     const int32_t* term_val;
     const int32_t* term_col;
     int64_t n_terms;  // U (zero terminal included)
+    int64_t n_ops;
     int64_t rows;
-    int Bw;           // words per slot
-    int G;            // lanes per item = Bw / VEC
+    int ldx, ldy;     // words per row of X / Y
+    int Bt;           // words per slot in one tile
+    int G;            // lanes per unit
+    int t0;           // first tile of the launch
 };
 
-// Child value: arena slot (>= 0) or terminal T[-c-1].
+struct LevelArgs {
+    const int2* ops;    // (left, right) references
+    const float* op_c;  // nullptr: all coefficients are 1
+    int64_t op_first;   // first arena slot of the level
+    int64_t n_ops;
+    const int32_t* em_src;
+    const int32_t* em_row;
+    int64_t em_first;
+    int64_t n_em;
+    const int32_t* seg_row;
+    const int64_t* seg_start;
+    int64_t seg_first;
+    int64_t n_seg;
+    int em_blocks;      // blocks [0, em_blocks) fold emissions, the rest evaluate ops
+    int em_chunk;       // emissions per lane group (chunked segmented mode)
+};
+
+template <int GLOG>
+__device__ __forceinline__ int64_t unit_of(int64_t t, int G) {
+    if constexpr (GLOG >= 0) return t >> GLOG;
+    else return t / G;
+}
+template <int GLOG>
+__device__ __forceinline__ int lane_of(int64_t t, int G) {
+    if constexpr (GLOG >= 0) return (int)(t & ((1 << GLOG) - 1));
+    else return (int)(t % G);
+}
+template <int GLOG>
+__device__ __forceinline__ int64_t items_of(int64_t units, int G) {
+    if constexpr (GLOG >= 0) return units << GLOG;
+    else return units * G;
+}
+
+// Per-tile view of the value space: arena slots (refs >= 0) and terminals
+// (refs < 0, T[-ref-1]); the address is selected without branching.
 template <class S, int VEC>
-__device__ __forceinline__ Vec<typename S::T, VEC> child(const SweepArgs& a, int32_t c, int lane_c) {
+struct Values {
     using T = typename S::T;
-    if (c >= 0) return vload_rw<T, VEC>(static_cast<const T*>(a.arena) + (int64_t)c * a.Bw + lane_c * VEC);
-    return vload_rw<T, VEC>(static_cast<const T*>(a.T) + (int64_t)(-(int64_t)c - 1) * a.Bw + lane_c * VEC);
+    const T* arena;
+    const T* term;
+    int Bt;
+    __device__ __forceinline__ Values(const SweepArgs& a, int tile)
+        : arena(static_cast<const T*>(a.arena) + (int64_t)tile * a.n_ops * a.Bt),
+          term(static_cast<const T*>(a.T) + (int64_t)tile * a.n_terms * a.Bt),
+          Bt(a.Bt) {}
+    __device__ __forceinline__ const T* addr(int32_t c, int lane) const {
+        const bool slot = c >= 0;
+        const int64_t idx = slot ? (int64_t)c : (-(int64_t)c - 1);
+        return (slot ? arena : term) + idx * Bt + lane * VEC;
+    }
+    __device__ __forceinline__ Vec<T, VEC> get(int32_t c, int lane) const { return vload_rw<T, VEC>(addr(c, lane)); }
+};
+
+template <class T>
+__device__ __forceinline__ T* yptr(const SweepArgs& a, int64_t row, int tile, int lane, int vec) {
+    return static_cast<T*>(a.Y) + row * a.ldy + (int64_t)tile * a.Bt + lane * vec;
 }
 
 // Prologue: Y = zero, T[0] = zero, T[q] = leaf(V[val], X[col]).
-template <class S, int VEC>
+template <class S, int VEC, int GLOG>
 __global__ void __launch_bounds__(256) k_prologue(SweepArgs a) {
     using T = typename S::T;
-    const int64_t ny = a.rows * a.G, nt = a.n_terms * a.G;
+    const int tile = a.t0 + blockIdx.y;
+    const int64_t ny = items_of<GLOG>(a.rows, a.G), nt = items_of<GLOG>(a.n_terms, a.G);
+    T* Tt = static_cast<T*>(a.T) + (int64_t)tile * a.n_terms * a.Bt;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ny + nt;
          t += (int64_t)gridDim.x * blockDim.x) {
         if (t < ny) {
-            int64_t r = t / a.G;
-            int c = (int)(t - r * a.G);
-            vstore<T, VEC>(static_cast<T*>(a.Y) + r * a.Bw + c * VEC, vzero<S, VEC>());
+            vstore<T, VEC>(yptr<T>(a, unit_of<GLOG>(t, a.G), tile, lane_of<GLOG>(t, a.G), VEC), vzero<S, VEC>());
         } else {
-            int64_t u = t - ny;
-            int64_t q = u / a.G;
-            int c = (int)(u - q * a.G);
+            const int64_t u = t - ny;
+            const int64_t q = unit_of<GLOG>(u, a.G);
+            const int lane = lane_of<GLOG>(u, a.G);
             Vec<T, VEC> out;
             if (q == 0) {
                 out = vzero<S, VEC>();
             } else {
                 float v = __ldg(a.V + __ldg(a.term_val + q - 1));
                 int32_t col = __ldg(a.term_col + q - 1);
-                Vec<T, VEC> x = vload<T, VEC>(static_cast<const T*>(a.X) + (int64_t)col * a.Bw + c * VEC);
+                Vec<T, VEC> x = vload<T, VEC>(static_cast<const T*>(a.X) + (int64_t)col * a.ldx +
+                                              (int64_t)tile * a.Bt + lane * VEC);
 #pragma unroll
                 for (int j = 0; j < VEC; ++j) out.v[j] = S::leaf(v, x.v[j]);
             }
-            vstore<T, VEC>(static_cast<T*>(a.T) + q * a.Bw + c * VEC, out);
+            vstore<T, VEC>(Tt + q * a.Bt + lane * VEC, out);
         }
     }
 }
 
-// Evaluate ops [0, n_ops) of one level: item t -> (op t / G, lane t % G).
-template <class S, int VEC>
-__device__ __forceinline__ void do_ops(const SweepArgs& a, const LevelArgs& L, int64_t t0, int64_t stride) {
+// Evaluate the ops of one level, two items per thread in flight.
+template <class S, int VEC, int GLOG>
+__device__ __forceinline__ void do_ops(const SweepArgs& a, const LevelArgs& L, int tile, int64_t t0,
+                                       int64_t stride) {
     using T = typename S::T;
-    const int64_t items = L.n_ops * a.G;
-    for (int64_t t = t0; t < items; t += stride) {
-        int64_t i = t / a.G;
-        int c = (int)(t - i * a.G);
-        int64_t s = L.op_first + i;
-        int32_t cl = __ldg(L.op_l + s), cr = __ldg(L.op_r + s);
-        Vec<T, VEC> lv = child<S, VEC>(a, cl, c);
-        Vec<T, VEC> rv = child<S, VEC>(a, cr, c);
+    const Values<S, VEC> val(a, tile);
+    T* out = static_cast<T*>(a.arena) + (int64_t)tile * a.n_ops * a.Bt;
+    const int64_t items = items_of<GLOG>(L.n_ops, a.G);
+    for (int64_t t = t0; t < items; t += 2 * stride) {
+        const int64_t tb = t + stride;
+        const bool hb = tb < items;
+        const int64_t sa = L.op_first + unit_of<GLOG>(t, a.G), sb = L.op_first + unit_of<GLOG>(hb ? tb : t, a.G);
+        const int la = lane_of<GLOG>(t, a.G), lb = lane_of<GLOG>(hb ? tb : t, a.G);
+        const int2 oa = __ldg(L.ops + sa), ob = __ldg(L.ops + sb);
+        Vec<T, VEC> la_v = val.get(oa.x, la), ra_v = val.get(oa.y, la);
+        Vec<T, VEC> lb_v = val.get(ob.x, lb), rb_v = val.get(ob.y, lb);
         if (L.op_c) {
-            float cf = __ldg(L.op_c + s);
+            const float ca = __ldg(L.op_c + sa), cb = __ldg(L.op_c + sb);
 #pragma unroll
-            for (int j = 0; j < VEC; ++j) lv.v[j] = S::apply(lv.v[j], cf);
+            for (int j = 0; j < VEC; ++j) {
+                la_v.v[j] = S::apply(la_v.v[j], ca);
+                lb_v.v[j] = S::apply(lb_v.v[j], cb);
+            }
         }
-        vstore<T, VEC>(static_cast<T*>(a.arena) + s * a.Bw + c * VEC, voplus<S, VEC>(lv, rv));
+        vstore<T, VEC>(out + sa * a.Bt + la * VEC, voplus<S, VEC>(la_v, ra_v));
+        if (hb) vstore<T, VEC>(out + sb * a.Bt + lb * VEC, voplus<S, VEC>(lb_v, rb_v));
     }
 }
 
 // One atomic per (emission, word): the reference's emit scheme.
-template <class S, int VEC>
-__device__ __forceinline__ void do_emits_atomic(const SweepArgs& a, const LevelArgs& L, int64_t t0,
+template <class S, int VEC, int GLOG>
+__device__ __forceinline__ void do_emits_atomic(const SweepArgs& a, const LevelArgs& L, int tile, int64_t t0,
                                                 int64_t stride) {
     using T = typename S::T;
-    const int64_t items = L.n_em * a.G;
+    const Values<S, VEC> val(a, tile);
+    const int64_t items = items_of<GLOG>(L.n_em, a.G);
     for (int64_t t = t0; t < items; t += stride) {
-        int64_t e = t / a.G;
-        int c = (int)(t - e * a.G);
-        int32_t src = __ldg(L.em_src + L.em_first + e);
-        int32_t row = __ldg(L.em_row + L.em_first + e);
-        vred<S, VEC>(static_cast<T*>(a.Y) + (int64_t)row * a.Bw + c * VEC, child<S, VEC>(a, src, c));
+        const int64_t e = L.em_first + unit_of<GLOG>(t, a.G);
+        const int lane = lane_of<GLOG>(t, a.G);
+        const int32_t src = __ldg(L.em_src + e), row = __ldg(L.em_row + e);
+        vred<S, VEC>(yptr<T>(a, row, tile, lane, VEC), val.get(src, lane));
     }
 }
 
-// Warp-segmented emits for G == 1: lane = emission; rows are sorted, so equal
-// rows are contiguous lanes; each segment is reduced and its first lane
-// issues one atomic.
-template <class S>
-__device__ __forceinline__ void do_emits_seg1(const SweepArgs& a, const LevelArgs& L, int64_t t0,
-                                              int64_t stride) {
+// Warp-segmented emits when G == 1: lane = emission; rows are sorted, so
+// equal rows are contiguous lanes; each segment is reduced in registers
+// (shuffles for (+,x), __reduce_*_sync for OR / min) and its first lane issues
+// one atomic per word.  Two warp-blocks are in flight per iteration.
+template <class S, int VEC>
+__device__ __forceinline__ Vec<typename S::T, VEC> warp_segment_reduce(Vec<typename S::T, VEC> v, unsigned peers,
+                                                                       int lane) {
     using T = typename S::T;
-    const int lane = threadIdx.x & 31;
-    const int64_t n = L.n_em;
-    // every lane of a warp runs the same number of iterations
-    for (int64_t base = t0 - lane; base < n; base += stride) {
-        int64_t e = base + lane;
-        bool valid = e < n;
-        int32_t row = valid ? __ldg(L.em_row + L.em_first + e) : -1 - lane;
-        T v = valid ? child<S, 1>(a, __ldg(L.em_src + L.em_first + e), 0).v[0] : S::zero();
-        unsigned peers = __match_any_sync(0xffffffffu, row);
-        T tot;
-        if constexpr (std::is_same<S, SBool>::value) {
-            tot = __reduce_or_sync(peers, v);
-        } else if constexpr (std::is_same<S, STrop>::value) {
-            tot = __reduce_min_sync(peers, v);
-        } else {
-            // suffix sums within the segment (segments are contiguous lanes)
-            const int last = 31 - __clz(peers);
-            tot = v;
+    Vec<T, VEC> tot;
+    if constexpr (std::is_same<S, SBool>::value) {
 #pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                T o = __shfl_down_sync(0xffffffffu, tot, d);
-                if (lane + d <= last) tot = S::oplus(tot, o);
+        for (int j = 0; j < VEC; ++j) tot.v[j] = __reduce_or_sync(peers, v.v[j]);
+    } else if constexpr (std::is_same<S, STrop>::value) {
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) tot.v[j] = __reduce_min_sync(peers, v.v[j]);
+    } else {
+        const int last = 31 - __clz(peers);  // segments are contiguous lanes
+        tot = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) {
+                T o = __shfl_down_sync(0xffffffffu, tot.v[j], d);
+                if (lane + d <= last) tot.v[j] = S::oplus(tot.v[j], o);
             }
         }
-        if (valid && lane == __ffs(peers) - 1) S::red(static_cast<T*>(a.Y) + (int64_t)row * a.Bw, tot);
+    }
+    return tot;
+}
+
+template <class S, int VEC>
+__device__ __forceinline__ void do_emits_warp(const SweepArgs& a, const LevelArgs& L, int tile, int64_t t0,
+                                              int64_t stride) {
+    using T = typename S::T;
+    const Values<S, VEC> val(a, tile);
+    const int lane = threadIdx.x & 31;
+    const int64_t n = L.n_em;
+    for (int64_t base = t0 - lane; base < n; base += 2 * stride) {  // warp-uniform trip count
+        const int64_t ea = base + lane, eb = base + stride + lane;
+        const bool va = ea < n, vb = eb < n;
+        const int32_t ra = va ? __ldg(L.em_row + L.em_first + ea) : -1 - lane;
+        const int32_t rb = vb ? __ldg(L.em_row + L.em_first + eb) : -1 - lane;
+        const int32_t sa = va ? __ldg(L.em_src + L.em_first + ea) : -1;
+        const int32_t sb = vb ? __ldg(L.em_src + L.em_first + eb) : -1;
+        Vec<T, VEC> xa = val.get(sa, 0), xb = val.get(sb, 0);  // ref -1 = the zero terminal
+        const unsigned pa = __match_any_sync(0xffffffffu, ra), pb = __match_any_sync(0xffffffffu, rb);
+        Vec<T, VEC> ta = warp_segment_reduce<S, VEC>(xa, pa, lane);
+        Vec<T, VEC> tb = warp_segment_reduce<S, VEC>(xb, pb, lane);
+        if (va && lane == __ffs(pa) - 1) vred<S, VEC>(yptr<T>(a, ra, tile, 0, VEC), ta);
+        if (vb && lane == __ffs(pb) - 1) vred<S, VEC>(yptr<T>(a, rb, tile, 0, VEC), tb);
     }
 }
 
-// Segmented emits for G > 1: each lane group walks em_chunk consecutive
-// emissions, accumulating while the row stays the same.
-template <class S, int VEC>
-__device__ __forceinline__ void do_emits_segG(const SweepArgs& a, const LevelArgs& L, int64_t t0,
-                                              int64_t stride) {
+// Chunked segmented emits: each lane group walks em_chunk consecutive
+// emissions (loads four ahead), accumulating while the row stays the same.
+template <class S, int VEC, int GLOG>
+__device__ __forceinline__ void do_emits_chunk(const SweepArgs& a, const LevelArgs& L, int tile, int64_t t0,
+                                               int64_t stride) {
     using T = typename S::T;
+    const Values<S, VEC> val(a, tile);
     const int64_t groups = (L.n_em + L.em_chunk - 1) / L.em_chunk;
-    const int64_t items = groups * a.G;
+    const int64_t items = items_of<GLOG>(groups, a.G);
+    const int32_t* rows = L.em_row + L.em_first;
+    const int32_t* srcs = L.em_src + L.em_first;
     for (int64_t t = t0; t < items; t += stride) {
-        int64_t g = t / a.G;
-        int c = (int)(t - g * a.G);
-        int64_t e0 = g * L.em_chunk, e1 = min(e0 + (int64_t)L.em_chunk, L.n_em);
-        const int32_t* rows = L.em_row + L.em_first;
-        const int32_t* srcs = L.em_src + L.em_first;
+        const int64_t g = unit_of<GLOG>(t, a.G);
+        const int lane = lane_of<GLOG>(t, a.G);
+        const int64_t e0 = g * L.em_chunk, e1 = min(e0 + (int64_t)L.em_chunk, L.n_em);
         int32_t cur = __ldg(rows + e0);
         Vec<T, VEC> acc = vzero<S, VEC>();
-        for (int64_t e = e0; e < e1; ++e) {
-            int32_t r = __ldg(rows + e);
-            Vec<T, VEC> v = child<S, VEC>(a, __ldg(srcs + e), c);
+        int64_t e = e0;
+        for (; e + 4 <= e1; e += 4) {
+            int32_t r[4], s[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                r[j] = __ldg(rows + e + j);
+                s[j] = __ldg(srcs + e + j);
+            }
+            Vec<T, VEC> v[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) v[j] = val.get(s[j], lane);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (r[j] != cur) {
+                    vred<S, VEC>(yptr<T>(a, cur, tile, lane, VEC), acc);
+                    acc = v[j];
+                    cur = r[j];
+                } else {
+                    acc = voplus<S, VEC>(acc, v[j]);
+                }
+            }
+        }
+        for (; e < e1; ++e) {
+            const int32_t r = __ldg(rows + e);
+            Vec<T, VEC> v = val.get(__ldg(srcs + e), lane);
             if (r != cur) {
-                vred<S, VEC>(static_cast<T*>(a.Y) + (int64_t)cur * a.Bw + c * VEC, acc);
+                vred<S, VEC>(yptr<T>(a, cur, tile, lane, VEC), acc);
                 acc = v;
                 cur = r;
             } else {
                 acc = voplus<S, VEC>(acc, v);
             }
         }
-        vred<S, VEC>(static_cast<T*>(a.Y) + (int64_t)cur * a.Bw + c * VEC, acc);
+        vred<S, VEC>(yptr<T>(a, cur, tile, lane, VEC), acc);
+    }
+}
+
+// Row-owned emits: one lane group folds a whole (level, row) segment and
+// updates its row of Y with a plain read-modify-write.  Within a launch every
+// (row, tile) belongs to exactly one segment and levels are separate launches,
+// so no atomics are needed and the (+,x) summation order is fixed.
+template <class S, int VEC, int GLOG>
+__device__ __forceinline__ void do_emits_rows(const SweepArgs& a, const LevelArgs& L, int tile, int64_t t0,
+                                              int64_t stride) {
+    using T = typename S::T;
+    const Values<S, VEC> val(a, tile);
+    const int64_t items = items_of<GLOG>(L.n_seg, a.G);
+    for (int64_t t = t0; t < items; t += stride) {
+        const int64_t s = L.seg_first + unit_of<GLOG>(t, a.G);
+        const int lane = lane_of<GLOG>(t, a.G);
+        const int64_t e0 = __ldg(L.seg_start + s), e1 = __ldg(L.seg_start + s + 1);
+        const int32_t row = __ldg(L.seg_row + s);
+        Vec<T, VEC> acc0 = vzero<S, VEC>(), acc1 = vzero<S, VEC>();
+        int64_t e = e0;
+        for (; e + 4 <= e1; e += 4) {
+            const int32_t s0 = __ldg(L.em_src + e), s1 = __ldg(L.em_src + e + 1);
+            const int32_t s2 = __ldg(L.em_src + e + 2), s3 = __ldg(L.em_src + e + 3);
+            Vec<T, VEC> v0 = val.get(s0, lane), v1 = val.get(s1, lane);
+            Vec<T, VEC> v2 = val.get(s2, lane), v3 = val.get(s3, lane);
+            acc0 = voplus<S, VEC>(acc0, voplus<S, VEC>(v0, v1));
+            acc1 = voplus<S, VEC>(acc1, voplus<S, VEC>(v2, v3));
+        }
+        for (; e < e1; ++e) acc0 = voplus<S, VEC>(acc0, val.get(__ldg(L.em_src + e), lane));
+        T* yp = yptr<T>(a, row, tile, lane, VEC);
+        vstore<T, VEC>(yp, voplus<S, VEC>(vload_rw<T, VEC>(yp), voplus<S, VEC>(acc0, acc1)));
     }
 }
 
 // One level launch: blocks [0, em_blocks) fold emissions, the rest evaluate ops.
-template <class S, int VEC, int EMIT>
+template <class S, int VEC, int GLOG, int EMIT>
 __global__ void __launch_bounds__(256) k_level(SweepArgs a, LevelArgs L) {
+    const int tile = a.t0 + blockIdx.y;
     if ((int)blockIdx.x < L.em_blocks) {
         const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
         const int64_t stride = (int64_t)L.em_blocks * blockDim.x;
-        if constexpr (EMIT == GMR_EMIT_ATOMIC) {
-            do_emits_atomic<S, VEC>(a, L, t0, stride);
-        } else {
-            if (a.G == 1) do_emits_seg1<S>(a, L, t0, stride);
-            else do_emits_segG<S, VEC>(a, L, t0, stride);
-        }
+        if constexpr (EMIT == GMR_EMIT_ATOMIC) do_emits_atomic<S, VEC, GLOG>(a, L, tile, t0, stride);
+        else if constexpr (EMIT == GMR_EMIT_ROWS) do_emits_rows<S, VEC, GLOG>(a, L, tile, t0, stride);
+        else if constexpr (GLOG == 0) do_emits_warp<S, VEC>(a, L, tile, t0, stride);
+        else do_emits_chunk<S, VEC, GLOG>(a, L, tile, t0, stride);
     } else {
         const int64_t t0 = (int64_t)(blockIdx.x - L.em_blocks) * blockDim.x + threadIdx.x;
         const int64_t stride = (int64_t)(gridDim.x - L.em_blocks) * blockDim.x;
-        do_ops<S, VEC>(a, L, t0, stride);
+        do_ops<S, VEC, GLOG>(a, L, tile, t0, stride);
     }
 }
 
@@ -358,13 +482,22 @@ static T* upload(const std::vector<T>& h, DevBuf& b) {
     return static_cast<T*>(b.p);
 }
 
+// Fully resolved launch configuration of one multiply.
+struct Launch {
+    int semiring, B, Bw, VEC, G, variant, emit, chunk;
+    int Bt, ntile, tile_levels;
+    bool operator==(const Launch& o) const {
+        return semiring == o.semiring && B == o.B && Bw == o.Bw && VEC == o.VEC && variant == o.variant &&
+               emit == o.emit && chunk == o.chunk && Bt == o.Bt && tile_levels == o.tile_levels;
+    }
+};
+
 struct GraphEntry {
     cudaGraphExec_t exec = nullptr;
-    int semiring = -1, B = 0, emit = 0, chunk = 0;
+    Launch lc{};
     int64_t launches = 0;  // kernel launches inside the graph
     const void* X = nullptr;
     void* Y = nullptr;
-    void* arena = nullptr;
 };
 
 }  // namespace gmr
@@ -374,14 +507,17 @@ struct gmr_engine {
     int rows = 0, cols = 0, depth = 0;
     int64_t n_ops = 0, n_terms = 0, n_em = 0;
     bool has_coeff = false;
-    std::vector<int64_t> lvl_off, em_off;
-    gmr::DevBuf op_l, op_r, op_c, em_src, em_row, term_val, term_col, V;
+    std::vector<int64_t> lvl_off, em_off, seg_off;
+    gmr::DevBuf ops, op_c, em_src, em_row, seg_row, seg_start, term_val, term_col, V;
     gmr::DevBuf arena, T, hX, hY;  // scratch
     cudaStream_t own_stream = nullptr;
     std::vector<gmr::GraphEntry> graphs;
     int64_t last_launches = 0;
     int sm_count = 152;
     std::mutex mu;
+    std::vector<gmr::DevBuf*> schedule_bufs() {
+        return {&ops, &op_c, &em_src, &em_row, &seg_row, &seg_start, &term_val, &term_col, &V};
+    }
 };
 
 namespace gmr {
@@ -401,19 +537,6 @@ struct DeviceGuard {
 
 static int words_per_slot(int semiring, int B) { return semiring == GMR_BOOLEAN ? (B + 31) / 32 : B; }
 
-static int pick_vec(int Bw, const void* X, const void* Y) {
-    auto aligned = [&](size_t a) {
-        return ((uintptr_t)X % a == 0) && ((uintptr_t)Y % a == 0);
-    };
-    if (Bw % 4 == 0 && aligned(16)) return 4;
-    if (Bw % 2 == 0 && aligned(8)) return 2;
-    return 1;
-}
-
-struct Launch {
-    int semiring, B, Bw, VEC, G, variant, emit, chunk;
-};
-
 // Optional per-launch timing: an event is recorded before the first launch
 // and after every launch.
 struct LaunchTimer {
@@ -431,7 +554,7 @@ struct LaunchTimer {
 };
 static thread_local LaunchTimer* t_timer = nullptr;
 
-template <class S, int VEC>
+template <class S, int VEC, int GLOG>
 static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void* Y, cudaStream_t st,
                            int64_t& launches) {
     if (t_timer) t_timer->mark();
@@ -444,34 +567,42 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
     a.term_val = static_cast<const int32_t*>(e->term_val.p);
     a.term_col = static_cast<const int32_t*>(e->term_col.p);
     a.n_terms = e->n_terms;
+    a.n_ops = e->n_ops;
     a.rows = e->rows;
-    a.Bw = lc.Bw;
+    a.ldx = lc.Bw;
+    a.ldy = lc.Bw;
+    a.Bt = lc.Bt;
     a.G = lc.G;
+    a.t0 = 0;
     const int TPB = 256;
-    auto blocks_for = [&](int64_t items) -> int {
+    auto blocks_for = [&](int64_t items, int nt) -> int {
         int64_t b = (items + TPB - 1) / TPB;
-        int64_t cap = (int64_t)e->sm_count * 64;  // grid-stride beyond this
+        int64_t cap = std::max<int64_t>(1, (int64_t)e->sm_count * 32 / nt);  // grid-stride beyond this
         return (int)std::max<int64_t>(1, std::min(b, cap));
+    };
+    auto after = [&] {
+        ++launches;
+        if (t_timer) t_timer->mark();
     };
     {
         int64_t items = (e->rows + e->n_terms) * (int64_t)lc.G;
-        k_prologue<S, VEC><<<blocks_for(items), TPB, 0, st>>>(a);
-        ++launches;
-        if (t_timer) t_timer->mark();
+        dim3 grid(blocks_for(items, lc.ntile), lc.ntile);
+        k_prologue<S, VEC, GLOG><<<grid, TPB, 0, st>>>(a);
+        after();
     }
-    auto em_items = [&](int64_t n) -> int64_t {
-        if (lc.emit == GMR_EMIT_ATOMIC || lc.G == 1) return n * lc.G;
-        return (n + lc.chunk - 1) / lc.chunk * lc.G;
-    };
-    auto launch_level = [&](int k_ops, int k_em, bool split) {
+    // ops of level k_ops (0: none) and emissions of level k_em (-1: none), tiles [t0, t0+nt)
+    auto level = [&](int k_ops, int k_em, int t0, int nt, bool split) {
+        SweepArgs s = a;
+        s.t0 = t0;
         LevelArgs L{};
-        L.op_l = static_cast<const int32_t*>(e->op_l.p);
-        L.op_r = static_cast<const int32_t*>(e->op_r.p);
+        L.ops = static_cast<const int2*>(e->ops.p);
         L.op_c = e->has_coeff ? static_cast<const float*>(e->op_c.p) : nullptr;
         L.em_src = static_cast<const int32_t*>(e->em_src.p);
         L.em_row = static_cast<const int32_t*>(e->em_row.p);
+        L.seg_row = static_cast<const int32_t*>(e->seg_row.p);
+        L.seg_start = static_cast<const int64_t*>(e->seg_start.p);
         L.em_chunk = lc.chunk;
-        int64_t nops = 0, nem = 0;
+        int64_t nops = 0, nem = 0, nseg = 0;
         if (k_ops >= 1) {
             L.op_first = e->lvl_off[k_ops - 1];
             nops = e->lvl_off[k_ops] - e->lvl_off[k_ops - 1];
@@ -479,39 +610,53 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
         if (k_em >= 0) {
             L.em_first = e->em_off[k_em];
             nem = e->em_off[k_em + 1] - e->em_off[k_em];
+            L.seg_first = e->seg_off[k_em];
+            nseg = e->seg_off[k_em + 1] - e->seg_off[k_em];
         }
-        auto go = [&](int64_t no, int64_t ne) {
+        auto em_items = [&]() -> int64_t {
+            if (lc.emit == GMR_EMIT_ATOMIC) return nem * lc.G;
+            if (lc.emit == GMR_EMIT_ROWS) return nseg * lc.G;
+            if (GLOG == 0) return (nem + 1) / 2;  // two warp-blocks per warp iteration
+            return (nem + lc.chunk - 1) / lc.chunk * lc.G;
+        };
+        auto go = [&](int64_t no, bool with_em) {
             LevelArgs M = L;
             M.n_ops = no;
-            M.n_em = ne;
-            if (no == 0 && ne == 0) return;
-            int eb = ne > 0 ? blocks_for(em_items(ne)) : 0;
-            int ob = no > 0 ? blocks_for(no * lc.G) : 0;
+            M.n_em = with_em ? nem : 0;
+            M.n_seg = with_em ? nseg : 0;
+            if (no == 0 && M.n_em == 0) return;
+            int eb = M.n_em > 0 ? blocks_for(em_items(), nt) : 0;
+            int ob = no > 0 ? blocks_for((no * lc.G + 1) / 2, nt) : 0;
             M.em_blocks = eb;
+            dim3 grid(eb + ob, nt);
             if (lc.emit == GMR_EMIT_ATOMIC)
-                k_level<S, VEC, GMR_EMIT_ATOMIC><<<eb + ob, TPB, 0, st>>>(a, M);
+                k_level<S, VEC, GLOG, GMR_EMIT_ATOMIC><<<grid, TPB, 0, st>>>(s, M);
+            else if (lc.emit == GMR_EMIT_ROWS)
+                k_level<S, VEC, GLOG, GMR_EMIT_ROWS><<<grid, TPB, 0, st>>>(s, M);
             else
-                k_level<S, VEC, GMR_EMIT_SEGMENTED><<<eb + ob, TPB, 0, st>>>(a, M);
-            ++launches;
-            if (t_timer) t_timer->mark();
+                k_level<S, VEC, GLOG, GMR_EMIT_SEGMENTED><<<grid, TPB, 0, st>>>(s, M);
+            after();
         };
         if (split) {  // plain: emissions and ops in separate launches
-            go(0, nem);
-            go(nops, 0);
+            go(0, true);
+            go(nops, false);
         } else {
-            go(nops, nem);
+            go(nops, true);
         }
     };
-    const bool plain = lc.variant == GMR_VARIANT_PLAIN;
-    if (plain) {
-        launch_level(0, 0, true);  // terminal emissions
-        for (int k = 1; k <= e->depth; ++k) {
-            launch_level(k, -1, true);
-            launch_level(0, k, true);
+    const int D = e->depth;
+    if (lc.variant == GMR_VARIANT_PLAIN) {
+        level(0, 0, 0, lc.ntile, true);  // terminal emissions
+        for (int k = 1; k <= D; ++k) {
+            level(k, -1, 0, lc.ntile, true);
+            level(0, k, 0, lc.ntile, true);
         }
     } else {
-        for (int k = 1; k <= e->depth; ++k) launch_level(k, k - 1, false);
-        launch_level(0, e->depth, false);
+        const int K = lc.ntile > 1 ? std::min(lc.tile_levels, D) : 0;
+        for (int t = 0; t < (K > 0 ? lc.ntile : 0); ++t)
+            for (int k = 1; k <= K; ++k) level(k, k - 1, t, 1, false);
+        for (int k = K + 1; k <= D; ++k) level(k, k - 1, 0, lc.ntile, false);
+        level(0, D, 0, lc.ntile, false);
     }
     GMR_CUDA(cudaGetLastError());
 }
@@ -519,9 +664,21 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
 template <class S>
 static void launch_chain_s(gmr_engine* e, const Launch& lc, const void* X, void* Y, cudaStream_t st,
                            int64_t& n) {
-    if (lc.VEC == 4) launch_chain_t<S, 4>(e, lc, X, Y, st, n);
-    else if (lc.VEC == 2) launch_chain_t<S, 2>(e, lc, X, Y, st, n);
-    else launch_chain_t<S, 1>(e, lc, X, Y, st, n);
+    if (lc.VEC == 4) {
+        switch (lc.G) {
+            case 1: return launch_chain_t<S, 4, 0>(e, lc, X, Y, st, n);
+            case 2: return launch_chain_t<S, 4, 1>(e, lc, X, Y, st, n);
+            case 4: return launch_chain_t<S, 4, 2>(e, lc, X, Y, st, n);
+            case 8: return launch_chain_t<S, 4, 3>(e, lc, X, Y, st, n);
+            case 16: return launch_chain_t<S, 4, 4>(e, lc, X, Y, st, n);
+            case 32: return launch_chain_t<S, 4, 5>(e, lc, X, Y, st, n);
+            default: return launch_chain_t<S, 4, -1>(e, lc, X, Y, st, n);
+        }
+    }
+    if (lc.VEC == 2 && lc.G == 1) return launch_chain_t<S, 2, 0>(e, lc, X, Y, st, n);
+    if (lc.VEC == 1 && lc.G == 1) return launch_chain_t<S, 1, 0>(e, lc, X, Y, st, n);
+    if (lc.VEC == 2) return launch_chain_t<S, 2, -1>(e, lc, X, Y, st, n);
+    return launch_chain_t<S, 1, -1>(e, lc, X, Y, st, n);
 }
 
 static void launch_chain(gmr_engine* e, const Launch& lc, const void* X, void* Y, cudaStream_t st, int64_t& n) {
@@ -530,19 +687,42 @@ static void launch_chain(gmr_engine* e, const Launch& lc, const void* X, void* Y
     else launch_chain_s<STrop>(e, lc, X, Y, st, n);
 }
 
+// Default tile width: the whole batch (measured: every extra tile pass costs
+// about as much as a full pass, the sweep is latency-bound per pass), split
+// only so that a tile is at most 128 words (32 lanes of 16-byte accesses).
+static int auto_tile(gmr_engine*, int Bw) {
+    int bt = Bw;
+    while (bt > 128 && bt % 2 == 0) bt /= 2;
+    return bt;
+}
+
 static Launch resolve_launch(gmr_engine* e, int semiring, int B, const void* X, void* Y, const gmr_config* cfg) {
     Launch lc{};
     lc.semiring = semiring;
     lc.B = B;
     lc.Bw = words_per_slot(semiring, B);
-    lc.VEC = pick_vec(lc.Bw, X, Y);
-    lc.G = lc.Bw / lc.VEC;
     lc.variant = cfg && cfg->variant ? cfg->variant : GMR_VARIANT_GRAPH;
+    if (lc.variant == GMR_VARIANT_PERSISTENT) lc.variant = GMR_VARIANT_GRAPH;  // not specialised yet
     lc.emit = cfg && cfg->emit_mode ? cfg->emit_mode : GMR_EMIT_SEGMENTED;
     if (lc.variant == GMR_VARIANT_PLAIN) lc.emit = GMR_EMIT_ATOMIC;
     lc.chunk = cfg && cfg->ops_per_cta > 0 ? cfg->ops_per_cta : 16;
-    if (lc.variant == GMR_VARIANT_PERSISTENT) lc.variant = GMR_VARIANT_GRAPH;  // not yet specialised
-    (void)e;
+    int bt = cfg && cfg->vec_tile > 0 ? cfg->vec_tile : auto_tile(e, lc.Bw);
+    if (bt > lc.Bw || lc.Bw % bt != 0) bt = lc.Bw;  // tiles must divide the batch
+    lc.Bt = bt;
+    lc.ntile = lc.Bw / bt;
+    lc.tile_levels = cfg && cfg->tile_levels > 0 ? cfg->tile_levels : e->depth;
+    if (!cfg || cfg->tile_levels <= 0) {
+        // tile the levels whose values overflow the budget at full width
+        int K = 0;
+        for (int k = 1; k <= e->depth; ++k)
+            if ((e->lvl_off[k] - e->lvl_off[k - 1]) * (int64_t)lc.Bw * 4 > (16ll << 20)) K = k;
+        lc.tile_levels = std::max(K, 1);
+    }
+    auto aligned = [&](size_t al) { return ((uintptr_t)X % al == 0) && ((uintptr_t)Y % al == 0); };
+    if (lc.Bt % 4 == 0 && lc.Bw % 4 == 0 && aligned(16)) lc.VEC = 4;
+    else if (lc.Bt % 2 == 0 && lc.Bw % 2 == 0 && aligned(8)) lc.VEC = 2;
+    else lc.VEC = 1;
+    lc.G = lc.Bt / lc.VEC;
     return lc;
 }
 
@@ -572,9 +752,7 @@ static void multiply_device(gmr_engine* e, int semiring, const void* X, void* Y,
     if (lc.variant == GMR_VARIANT_GRAPH) {
         GraphEntry* hit = nullptr;
         for (auto& g : e->graphs)
-            if (g.exec && g.semiring == semiring && g.B == B && g.X == X && g.Y == Y && g.arena == e->arena.p &&
-                g.emit == lc.emit && g.chunk == lc.chunk)
-                hit = &g;
+            if (g.exec && g.lc == lc && g.X == X && g.Y == Y) hit = &g;
         if (!hit) {
             if (e->graphs.size() >= 8) {
                 cudaGraphExecDestroy(e->graphs.front().exec);
@@ -595,13 +773,9 @@ static void multiply_device(gmr_engine* e, int semiring, const void* X, void* Y,
             cudaError_t ie = cudaGraphInstantiate(&ge.exec, graph, 0);
             cudaGraphDestroy(graph);
             GMR_CUDA(ie);
-            ge.semiring = semiring;
-            ge.B = B;
+            ge.lc = lc;
             ge.X = X;
             ge.Y = Y;
-            ge.arena = e->arena.p;
-            ge.emit = lc.emit;
-            ge.chunk = lc.chunk;
             ge.launches = n;
             e->graphs.push_back(ge);
             hit = &e->graphs.back();
@@ -655,20 +829,25 @@ extern "C" int gmr_engine_create(const gmr_plan* p, int device, gmr_engine** out
         e->has_coeff = p->has_coeff();
         e->lvl_off = p->lvl_off;
         e->em_off = p->em_off;
+        e->seg_off = p->seg_off;
         try {
-            upload(p->op_l, e->op_l);
-            upload(p->op_r, e->op_r);
+            {
+                std::vector<int2> ops((size_t)p->n_ops());
+                for (int64_t i = 0; i < p->n_ops(); ++i) ops[i] = make_int2(p->op_l[i], p->op_r[i]);
+                upload(ops, e->ops);
+            }
             if (e->has_coeff) upload(p->op_c, e->op_c);
             upload(p->em_src, e->em_src);
             upload(p->em_row, e->em_row);
+            upload(p->seg_row, e->seg_row);
+            upload(p->seg_start, e->seg_start);
             upload(p->term_val, e->term_val);
             upload(p->term_col, e->term_col);
             upload(p->V, e->V);
             GMR_CUDA(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking));
             GMR_CUDA(cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, device));
         } catch (...) {
-            for (auto* b : {&e->op_l, &e->op_r, &e->op_c, &e->em_src, &e->em_row, &e->term_val, &e->term_col, &e->V})
-                b->release();
+            for (auto* b : e->schedule_bufs()) b->release();
             if (e->own_stream) cudaStreamDestroy(e->own_stream);
             throw;
         }
@@ -738,9 +917,9 @@ extern "C" int64_t gmr_engine_last_launches(const gmr_engine* e) { return e ? e-
 extern "C" int64_t gmr_engine_device_bytes(const gmr_engine* e) {
     if (!e) return -1;
     int64_t t = 0;
-    for (auto* b : {&e->op_l, &e->op_r, &e->op_c, &e->em_src, &e->em_row, &e->term_val, &e->term_col, &e->V,
-                    &e->arena, &e->T, &e->hX, &e->hY})
-        t += (int64_t)b->bytes;
+    auto bufs = const_cast<gmr_engine*>(e)->schedule_bufs();
+    for (auto* b : {&e->arena, &e->T, &e->hX, &e->hY}) bufs.push_back(const_cast<DevBuf*>(b));
+    for (auto* b : bufs) t += (int64_t)b->bytes;
     return t;
 }
 
@@ -752,9 +931,8 @@ extern "C" void gmr_engine_free(gmr_engine* e) {
         cudaSetDevice(e->device);
         for (auto& g : e->graphs)
             if (g.exec) cudaGraphExecDestroy(g.exec);
-        for (auto* b : {&e->op_l, &e->op_r, &e->op_c, &e->em_src, &e->em_row, &e->term_val, &e->term_col, &e->V,
-                        &e->arena, &e->T, &e->hX, &e->hY})
-            b->release();
+        for (auto* b : e->schedule_bufs()) b->release();
+        for (auto* b : {&e->arena, &e->T, &e->hX, &e->hY}) b->release();
         if (e->own_stream) cudaStreamDestroy(e->own_stream);
         if (prev >= 0) cudaSetDevice(prev);
     }

@@ -79,6 +79,12 @@ struct gmr_plan {
     std::vector<float> op_c;                  // empty unless has_coeff
     std::vector<int64_t> em_off;              // depth + 2
     std::vector<int32_t> em_src, em_row;
+    // Row segments: the emissions of one (level, row) pair are contiguous;
+    // segment s covers [seg_start[s], seg_start[s+1]) of em_src and folds
+    // into row seg_row[s].  Level k's segments are [seg_off[k], seg_off[k+1]).
+    std::vector<int64_t> seg_off;             // depth + 2
+    std::vector<int32_t> seg_row;             // n_seg
+    std::vector<int64_t> seg_start;           // n_seg + 1
     gmr_plan_stats stats{};
 
     int64_t n_ops() const { return (int64_t)op_l.size(); }

@@ -52,6 +52,8 @@ std::vector<int64_t> child_sort(const std::vector<int32_t>& L, const std::vector
     return perm;
 }
 
+void build_segments(gmr_plan& p);
+
 // Group emissions by level, then sort each level's segment by (row, src).
 void finish_emissions(gmr_plan& p, std::vector<int32_t>& lvl_of_em, std::vector<int32_t>& src,
                       std::vector<int32_t>& row) {
@@ -96,6 +98,26 @@ void finish_emissions(gmr_plan& p, std::vector<int32_t>& lvl_of_em, std::vector<
                 break;
             }
     }
+    build_segments(p);
+}
+
+// Row segments of the (level-major, row-sorted) emission arrays.
+void build_segments(gmr_plan& p) {
+    const int D = p.depth;
+    p.seg_off.assign(D + 2, 0);
+    p.seg_row.clear();
+    p.seg_start.clear();
+    for (int k = 0; k <= D; ++k) {
+        p.seg_off[k] = (int64_t)p.seg_row.size();
+        for (int64_t e = p.em_off[k]; e < p.em_off[k + 1]; ++e) {
+            if (e == p.em_off[k] || p.em_row[e] != p.em_row[e - 1]) {
+                p.seg_row.push_back(p.em_row[e]);
+                p.seg_start.push_back(e);
+            }
+        }
+    }
+    p.seg_off[D + 1] = (int64_t)p.seg_row.size();
+    p.seg_start.push_back((int64_t)p.em_src.size());
 }
 
 void fill_common_stats(gmr_plan& p) {
@@ -141,6 +163,19 @@ void validate_plan(const gmr_plan& p) {
             if (k == 0 && c >= 0) ok = false;
             if (!ok) throw Error(GMR_ERR_FORMAT, "plan: emission source out of range");
             if (p.em_row[e] < 0 || p.em_row[e] >= p.rows) throw Error(GMR_ERR_FORMAT, "plan: emission row out of range");
+        }
+    }
+    if ((int)p.seg_off.size() != D + 2 || p.seg_start.size() != p.seg_row.size() + 1 ||
+        p.seg_off[D + 1] != (int64_t)p.seg_row.size() || p.seg_start.back() != (int64_t)p.em_src.size())
+        throw Error(GMR_ERR_FORMAT, "plan: bad row segments");
+    for (int k = 0; k <= D; ++k) {
+        for (int64_t q = p.seg_off[k]; q < p.seg_off[k + 1]; ++q) {
+            if (p.seg_start[q] < p.em_off[k] || p.seg_start[q + 1] > p.em_off[k + 1] || p.seg_start[q + 1] <= p.seg_start[q])
+                throw Error(GMR_ERR_FORMAT, "plan: row segment out of its level");
+            if (q > p.seg_off[k] && p.seg_row[q] <= p.seg_row[q - 1])
+                throw Error(GMR_ERR_FORMAT, "plan: row segments not strictly increasing");
+            for (int64_t e = p.seg_start[q]; e < p.seg_start[q + 1]; ++e)
+                if (p.em_row[e] != p.seg_row[q]) throw Error(GMR_ERR_FORMAT, "plan: row segment mixes rows");
         }
     }
     for (size_t q = 0; q < p.term_val.size(); ++q) {
@@ -507,6 +542,9 @@ extern "C" int gmr_plan_array(const gmr_plan* p, int which, const void** ptr, in
             case 7: *ptr = p->term_val.data(); *n = (int64_t)p->term_val.size(); break;
             case 8: *ptr = p->term_col.data(); *n = (int64_t)p->term_col.size(); break;
             case 9: *ptr = p->V.data(); *n = (int64_t)p->V.size(); break;
+            case 10: *ptr = p->seg_off.data(); *n = (int64_t)p->seg_off.size(); break;
+            case 11: *ptr = p->seg_row.data(); *n = (int64_t)p->seg_row.size(); break;
+            case 12: *ptr = p->seg_start.data(); *n = (int64_t)p->seg_start.size(); break;
             default: throw Error(GMR_ERR_ARG, "unknown plan array");
         }
     });

@@ -29,7 +29,7 @@ SEMIRINGS = {"plustimes": PLUS_TIMES, "boolean": BOOLEAN, "bool": BOOLEAN, "trop
 TROPICAL_INF = 1_000_000_000
 
 VARIANT_AUTO, VARIANT_PLAIN, VARIANT_FUSED, VARIANT_GRAPH, VARIANT_PERSISTENT = 0, 1, 2, 3, 4
-EMIT_AUTO, EMIT_ATOMIC, EMIT_SEGMENTED = 0, 1, 2
+EMIT_AUTO, EMIT_ATOMIC, EMIT_SEGMENTED, EMIT_ROWS = 0, 1, 2, 3
 
 __all__ = [
     "GmrError", "Csrv", "Grammar", "Plan", "Engine", "gen_mosaic", "gen_copy_graph", "repair", "semiring_id",
@@ -310,7 +310,8 @@ class Plan:
 
     _ARRAYS = {"op_l": (0, np.int32), "op_r": (1, np.int32), "op_c": (2, np.float32), "lvl_off": (3, np.int64),
                "em_off": (4, np.int64), "em_src": (5, np.int32), "em_row": (6, np.int32),
-               "term_val": (7, np.int32), "term_col": (8, np.int32), "V": (9, np.float32)}
+               "term_val": (7, np.int32), "term_col": (8, np.int32), "V": (9, np.float32),
+               "seg_off": (10, np.int64), "seg_row": (11, np.int32), "seg_start": (12, np.int64)}
 
     def array(self, name: str) -> np.ndarray:
         which, dt = self._ARRAYS[name]
@@ -400,8 +401,8 @@ class Engine:
         self.close()
 
     @staticmethod
-    def _cfg(variant=0, emit_mode=0, ops_per_cta=0, vec_tile=0):
-        return Config(variant, vec_tile, ops_per_cta, emit_mode)
+    def _cfg(variant=0, emit_mode=0, ops_per_cta=0, vec_tile=0, tile_levels=0):
+        return Config(variant, vec_tile, ops_per_cta, emit_mode, tile_levels)
 
     def multiply_device(self, semiring, x_ptr: int, y_ptr: int, B: int, stream: int = 0, **cfg):
         c = self._cfg(**cfg)

@@ -199,7 +199,9 @@ double gmr_plan_alg_bytes(const gmr_plan* p, int semiring, int B);
  * which = 0 op_l, 1 op_r (int32 references: >= 0 arena slot, < 0 terminal
  * -ref-1), 2 op_c (float, absent unless run-length rules exist), 3 lvl_off
  * (int64, depth+1), 4 em_off (int64, depth+2), 5 em_src (int32),
- * 6 em_row (int32), 7 term_val (int32), 8 term_col (int32), 9 V (float).
+ * 6 em_row (int32), 7 term_val (int32), 8 term_col (int32), 9 V (float),
+ * 10 seg_off (int64, depth+2), 11 seg_row (int32), 12 seg_start (int64,
+ * n_seg+1): the emissions of one (level, row) pair form one row segment.
  * *ptr stays valid until gmr_plan_free. */
 int gmr_plan_array(const gmr_plan* p, int which, const void** ptr, int64_t* n);
 /* Human-readable per-level report (the host_scheduler inspector). */
@@ -214,18 +216,26 @@ typedef struct gmr_engine gmr_engine;
 /* Kernel-variant knobs; 0 = let the engine choose. */
 typedef struct {
     int variant;      /* GMR_VARIANT_* */
-    int vec_tile;     /* right-hand sides per sweep tile (0 = all B) */
-    int ops_per_cta;  /* work items per CTA hint */
+    int vec_tile;     /* words per right-hand-side tile (must divide the
+                         batch's words; 0 = engine default) */
+    int ops_per_cta;  /* emissions per lane group in GMR_EMIT_SEGMENTED */
     int emit_mode;    /* GMR_EMIT_* */
+    int tile_levels;  /* levels 1..tile_levels run tile by tile, the rest
+                         all tiles per launch (0 = by level size) */
 } gmr_config;
 enum {
     GMR_VARIANT_AUTO = 0,
     GMR_VARIANT_PLAIN = 1,   /* per-level launches, one atomic per emission */
-    GMR_VARIANT_FUSED = 2,   /* per-level launches, ops+emits fused, segmented emits */
+    GMR_VARIANT_FUSED = 2,   /* per-level launches, ops+emits fused */
     GMR_VARIANT_GRAPH = 3,   /* FUSED captured once into a CUDA graph */
     GMR_VARIANT_PERSISTENT = 4 /* one cooperative launch walks every level */
 };
-enum { GMR_EMIT_AUTO = 0, GMR_EMIT_ATOMIC = 1, GMR_EMIT_SEGMENTED = 2 };
+enum {
+    GMR_EMIT_AUTO = 0,
+    GMR_EMIT_ATOMIC = 1,     /* one atomic per (emission, word) */
+    GMR_EMIT_SEGMENTED = 2,  /* warp/chunk segmented reduction, one atomic per segment */
+    GMR_EMIT_ROWS = 3        /* row-owned segments, plain read-modify-write */
+};
 
 int gmr_engine_create(const gmr_plan* p, int device, gmr_engine** out);
 /* dX, dY: device pointers (layouts above). stream: cudaStream_t or NULL. */

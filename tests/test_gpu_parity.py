@@ -92,6 +92,16 @@ def test_golden_single_vector(case, sr, variant):
     assert eng.last_launches > 0
 
 
+CONFIGS = [
+    dict(variant=gmr.VARIANT_PLAIN),                                       # reference scheme
+    dict(variant=gmr.VARIANT_GRAPH),                                       # engine default
+    dict(variant=gmr.VARIANT_FUSED, emit_mode=gmr.EMIT_SEGMENTED),
+    dict(variant=gmr.VARIANT_FUSED, emit_mode=gmr.EMIT_ATOMIC, vec_tile=2),
+    dict(variant=gmr.VARIANT_GRAPH, emit_mode=gmr.EMIT_ROWS, vec_tile=4, tile_levels=2),
+    dict(variant=gmr.VARIANT_GRAPH, emit_mode=gmr.EMIT_SEGMENTED, vec_tile=8, ops_per_cta=5),
+]
+
+
 @pytest.mark.parametrize("sr", range(3))
 @pytest.mark.parametrize("B", [2, 3, 8, 32, 33, 64, 128])
 def test_golden_batched(case, sr, B):
@@ -99,8 +109,8 @@ def test_golden_batched(case, sr, B):
     X = random_X(sr, cols, B, 100 + B)
     ref = oracle_columns(case["sched"], sr, case["V"], X, rows, cols)
     eng = gmr.Engine(case["plan"])
-    for variant in (gmr.VARIANT_PLAIN, gmr.VARIANT_GRAPH):
-        Y = engine_outputs(sr, eng.multiply(engine_inputs(sr, X), sr, B=B, variant=variant), B)
+    for cfg in CONFIGS:
+        Y = engine_outputs(sr, eng.multiply(engine_inputs(sr, X), sr, B=B, **cfg), B)
         check(sr, Y, ref)
 
 
@@ -219,10 +229,11 @@ def test_c1_plain_spmv_vs_fp64(c1):
 def test_c1_batched_vs_fp64(c1, B):
     rng = np.random.default_rng(B)
     X = rng.uniform(-1, 1, (5000, B)).astype(np.float32)
-    Y = c1["eng"].multiply(X, 0, B=B)
-    for b in range(0, B, max(1, B // 4)):
-        ref = c1["sched"].sweep_f64(0, c1["V"], X[:, b], 20000, 5000)
-        assert relmax(Y[:, b], ref) <= TOL
+    refs = {b: c1["sched"].sweep_f64(0, c1["V"], X[:, b], 20000, 5000) for b in range(0, B, max(1, B // 4))}
+    for cfg in CONFIGS:
+        Y = c1["eng"].multiply(X, 0, B=B, **cfg)
+        for b, ref in refs.items():
+            assert relmax(Y[:, b], ref) <= TOL, cfg
 
 
 def test_c1_properties(c1):
