@@ -939,6 +939,141 @@ extern "C" void gmr_engine_free(gmr_engine* e) {
     delete e;
 }
 
+// ------------------------------------------------------------------ no-allocation entry point
+// For callers that may not allocate device memory while they run: the
+// scratch values live in this statically sized device array instead of
+// engine-owned cudaMalloc buffers; the schedule, X and Y are the caller's.
+namespace gmr {
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[GMR_NOALLOC_SCRATCH_BYTES];
+
+// Device address of g_noalloc_scratch per device.  In host code the symbol
+// name is only a host-side stand-in, so the address is looked up once per
+// device with that device current.
+static void* g_noalloc_addr[64] = {};
+static std::mutex g_noalloc_mu;
+
+static void* noalloc_scratch_for_current_device() {
+    int dev = -1;
+    GMR_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) throw Error(GMR_ERR_RANGE, "device index beyond 63");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* ptr = nullptr;
+        GMR_CUDA(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
+        g_noalloc_addr[dev] = ptr;
+    }
+    return g_noalloc_addr[dev];
+}
+
+template <class S, int VEC, int GLOG>
+static void noalloc_chain(const gmr_device_plan& p, void* arena, void* T, int Bw, int G, const void* X, void* Y,
+                          cudaStream_t st, int sm_count) {
+    SweepArgs a;
+    a.arena = arena;
+    a.T = T;
+    a.Y = Y;
+    a.X = X;
+    a.V = p.V;
+    a.term_val = p.term_val;
+    a.term_col = p.term_col;
+    a.n_terms = p.n_terms;
+    a.n_ops = p.n_ops;
+    a.rows = p.rows;
+    a.ldx = Bw;
+    a.ldy = Bw;
+    a.Bt = Bw;
+    a.G = G;
+    a.t0 = 0;
+    const int TPB = 256;
+    auto blocks_for = [&](int64_t items) -> int {
+        int64_t b = (items + TPB - 1) / TPB;
+        return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)sm_count * 32));
+    };
+    k_prologue<S, VEC, GLOG><<<dim3(blocks_for((p.rows + p.n_terms) * (int64_t)G), 1), TPB, 0, st>>>(a);
+    for (int k = 1; k <= p.depth + 1; ++k) {  // ops of level k (none for k = depth + 1), emissions of k - 1
+        LevelArgs L{};
+        L.ops = reinterpret_cast<const int2*>(p.ops);
+        L.op_c = p.op_c;
+        L.em_src = p.em_src;
+        L.seg_row = p.seg_row;
+        L.seg_start = p.seg_start;
+        if (k <= p.depth) {
+            L.op_first = p.lvl_off[k - 1];
+            L.n_ops = p.lvl_off[k] - p.lvl_off[k - 1];
+        }
+        L.seg_first = p.seg_off[k - 1];
+        L.n_seg = p.seg_off[k] - p.seg_off[k - 1];
+        L.n_em = L.n_seg;
+        if (L.n_ops == 0 && L.n_seg == 0) continue;
+        const int eb = L.n_seg > 0 ? blocks_for(L.n_seg * G) : 0;
+        const int ob = L.n_ops > 0 ? blocks_for((L.n_ops * G + 1) / 2) : 0;
+        L.em_blocks = eb;
+        k_level<S, VEC, GLOG, GMR_EMIT_ROWS><<<dim3(eb + ob, 1), TPB, 0, st>>>(a, L);
+    }
+    GMR_CUDA(cudaGetLastError());
+}
+
+template <class S>
+static void noalloc_dispatch(const gmr_device_plan& p, void* arena, void* T, int Bw, const void* X, void* Y,
+                             cudaStream_t st, int sm_count) {
+    const bool a16 = ((uintptr_t)X % 16 == 0) && ((uintptr_t)Y % 16 == 0);
+    const bool a8 = ((uintptr_t)X % 8 == 0) && ((uintptr_t)Y % 8 == 0);
+    if (Bw % 4 == 0 && a16) {
+        switch (Bw / 4) {
+            case 1: return noalloc_chain<S, 4, 0>(p, arena, T, Bw, 1, X, Y, st, sm_count);
+            case 2: return noalloc_chain<S, 4, 1>(p, arena, T, Bw, 2, X, Y, st, sm_count);
+            case 4: return noalloc_chain<S, 4, 2>(p, arena, T, Bw, 4, X, Y, st, sm_count);
+            case 8: return noalloc_chain<S, 4, 3>(p, arena, T, Bw, 8, X, Y, st, sm_count);
+            case 16: return noalloc_chain<S, 4, 4>(p, arena, T, Bw, 16, X, Y, st, sm_count);
+            case 32: return noalloc_chain<S, 4, 5>(p, arena, T, Bw, 32, X, Y, st, sm_count);
+            default: return noalloc_chain<S, 4, -1>(p, arena, T, Bw, Bw / 4, X, Y, st, sm_count);
+        }
+    }
+    if (Bw == 2 && a8) return noalloc_chain<S, 2, 0>(p, arena, T, Bw, 1, X, Y, st, sm_count);
+    if (Bw == 1) return noalloc_chain<S, 1, 0>(p, arena, T, Bw, 1, X, Y, st, sm_count);
+    return noalloc_chain<S, 1, -1>(p, arena, T, Bw, Bw, X, Y, st, sm_count);
+}
+
+}  // namespace gmr
+
+extern "C" int gmr_multiply_noalloc(const gmr_device_plan* p, int semiring, const void* dX, void* dY, int B,
+                                    void* stream) {
+    return guarded([&] {
+        if (!p) throw Error(GMR_ERR_ARG, "null plan");
+        if (semiring < 0 || semiring > 2) throw Error(GMR_ERR_ARG, "unknown semiring");
+        if (B < 1) throw Error(GMR_ERR_ARG, "B must be >= 1");
+        if (p->depth < 0 || p->n_ops < 0 || p->n_terms < 1 || p->rows < 0 || p->cols < 1)
+            throw Error(GMR_ERR_ARG, "bad plan sizes");
+        if (!p->lvl_off || !p->seg_off || (p->n_ops > 0 && !p->ops) || !p->seg_start || (p->n_terms > 1 &&
+            (!p->term_val || !p->term_col || !p->V)))
+            throw Error(GMR_ERR_ARG, "null plan array");
+        if ((!dX && p->cols > 0) || (!dY && p->rows > 0)) throw Error(GMR_ERR_ARG, "null X or Y");
+        if (((uintptr_t)dX | (uintptr_t)dY) % 4 != 0 || (uintptr_t)p->ops % 8 != 0 || (uintptr_t)p->seg_start % 8 != 0)
+            throw Error(GMR_ERR_ARG, "misaligned device pointer");
+        if (p->lvl_off[0] != 0 || p->lvl_off[p->depth] != p->n_ops)
+            throw Error(GMR_ERR_FORMAT, "level offsets do not cover the rules");
+        const int Bw = words_per_slot(semiring, B);
+        const uint64_t arena_bytes = ((uint64_t)p->n_ops * Bw * 4 + 255) / 256 * 256;
+        const uint64_t need = arena_bytes + (uint64_t)p->n_terms * Bw * 4;
+        if (need > GMR_NOALLOC_SCRATCH_BYTES)
+            throw Error(GMR_ERR_RANGE, "scratch of " + std::to_string(need) + " bytes ((n_ops + n_terms) x " +
+                                           std::to_string(Bw) + " words x 4) exceeds the static " +
+                                           std::to_string((unsigned long long)GMR_NOALLOC_SCRATCH_BYTES) +
+                                           "-byte array; use gmr_engine_multiply");
+        unsigned char* base = static_cast<unsigned char*>(noalloc_scratch_for_current_device());
+        int dev = 0, sms = 152;
+        GMR_CUDA(cudaGetDevice(&dev));
+        GMR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        void* arena = base;
+        void* T = base + arena_bytes;
+        if (semiring == GMR_PLUS_TIMES) noalloc_dispatch<SPlus>(*p, arena, T, Bw, dX, dY, st, sms);
+        else if (semiring == GMR_BOOLEAN) noalloc_dispatch<SBool>(*p, arena, T, Bw, dX, dY, st, sms);
+        else noalloc_dispatch<STrop>(*p, arena, T, Bw, dX, dY, st, sms);
+    });
+}
+
 // ------------------------------------------------------------------ legacy ABI
 // The reference's two entry points (gpu_engine.h:239-276).  Per call: relayout
 // the given proper-layered schedule into a plan, upload, run `iters`

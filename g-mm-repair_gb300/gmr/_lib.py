@@ -51,6 +51,16 @@ class PlanStats(C.Structure):
     ]
 
 
+class DevicePlan(C.Structure):
+    """gmr_device_plan of include/gmr.h"""
+    _fields_ = [
+        ("rows", C.c_int), ("cols", C.c_int), ("depth", C.c_int), ("n_ops", C.c_int64), ("n_terms", C.c_int64),
+        ("lvl_off", C.c_void_p), ("seg_off", C.c_void_p), ("ops", C.c_void_p), ("op_c", C.c_void_p),
+        ("em_src", C.c_void_p), ("seg_row", C.c_void_p), ("seg_start", C.c_void_p), ("term_val", C.c_void_p),
+        ("term_col", C.c_void_p), ("V", C.c_void_p),
+    ]
+
+
 class Config(C.Structure):
     _fields_ = [("variant", C.c_int), ("vec_tile", C.c_int), ("ops_per_cta", C.c_int), ("emit_mode", C.c_int),
                 ("tile_levels", C.c_int)]
@@ -103,6 +113,7 @@ _SIGS = {
     "gmr_engine_last_launches": (C.c_int64, [P]),
     "gmr_engine_device_bytes": (C.c_int64, [P]),
     "gmr_engine_free": (None, [P]),
+    "gmr_multiply_noalloc": (C.c_int, [C.POINTER(DevicePlan), C.c_int, P, P, C.c_int, P]),
     "run_gpu_right_multiply_layered": (None, [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(LayeredRule), I32P,
                                               I32P, F32P, C.c_int, F32P, C.POINTER(GPUSchedule), F32P, C.c_int]),
     "run_gpu_right_multiply_batched": (None, [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(LayeredRule), I32P,

@@ -286,6 +286,49 @@ void run_gpu_right_multiply_batched(
     const GPUSchedule* h_sched, float* h_Y, int B, int iters);
 #endif
 
+/* ------------------------------------------------------------------ */
+/* Multiply without any allocation                                      */
+/* ------------------------------------------------------------------ */
+/* No counterpart in the reference.  For callers that are not allowed to
+ * allocate device memory while they run -- code that executes while another
+ * component owns the device allocator (a serving loop with a fixed memory
+ * budget, a memory pool that must not grow, work issued between allocator
+ * checkpoints) -- this entry point multiplies without calling cudaMalloc,
+ * cudaFree or any allocating routine.  The caller keeps the schedule in device
+ * memory it obtained its own way (copy the arrays that gmr_plan_array returns)
+ * and passes inputs and outputs.  The scratch values (one arena slot per
+ * evaluated rule plus the terminal table, (n_ops + n_terms) * words * 4 bytes
+ * with words = B, or ceil(B/32) for GMR_BOOLEAN) live in one statically sized
+ * device array of GMR_NOALLOC_SCRATCH_BYTES (64 MiB) that every GPU loading
+ * the library holds until the process exits.  Larger requests fail with
+ * GMR_ERR_RANGE before anything is launched.
+ *
+ * The first call on a device looks the array up (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture.
+ * Every call shares the one array: calls that overlap on the GPU (different
+ * streams, or host threads without ordering) race on it and give wrong
+ * results; serialize them.  Nothing in the array needs to start at zero:
+ * every value is written before it is read within a call.  Launches are the
+ * fused per-level kernels with row-owned emission folding, on `stream`. */
+#define GMR_NOALLOC_SCRATCH_BYTES (64ull << 20)
+typedef struct {
+    int rows, cols, depth;
+    int64_t n_ops;            /* evaluated rules */
+    int64_t n_terms;          /* terminals U, zero terminal included */
+    const int64_t* lvl_off;   /* HOST, depth + 1 (gmr_plan_array 3) */
+    const int64_t* seg_off;   /* HOST, depth + 2 (gmr_plan_array 10) */
+    const int32_t* ops;       /* device, 2 * n_ops: (op_l[i], op_r[i]) pairs, 8-byte aligned */
+    const float* op_c;        /* device, n_ops, or NULL when all coefficients are 1 */
+    const int32_t* em_src;    /* device (gmr_plan_array 5) */
+    const int32_t* seg_row;   /* device (gmr_plan_array 11) */
+    const int64_t* seg_start; /* device (gmr_plan_array 12) */
+    const int32_t* term_val;  /* device, n_terms - 1 */
+    const int32_t* term_col;  /* device, n_terms - 1 */
+    const float* V;           /* device */
+} gmr_device_plan;
+int gmr_multiply_noalloc(const gmr_device_plan* p, int semiring, const void* dX, void* dY,
+                         int B, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
