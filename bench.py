@@ -200,7 +200,9 @@ def main():
     ap.add_argument("--impl", choices=["gmr", "reference"], default="gmr")
     ap.add_argument("--workload", choices=list(WORKLOADS), default="mosaic-200000x10000")
     ap.add_argument("--B", type=int, default=32)
-    ap.add_argument("--variant", type=int, default=3, help="1 plain, 2 fused, 3 graph")
+    ap.add_argument("--variant", type=int, default=0,
+                    help="0 auto (autotuned per-launch table, CUDA graph), 1 plain, 2 fused, 3 graph")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (AUTO = engine defaults)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-seconds", type=float, default=6.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -244,6 +246,27 @@ def main():
     def step():
         eng.multiply_device(0, X.data_ptr(), Y.data_ptr(), B, stream=sp, **cfg)
 
+    def timed(n, **c):
+        for _ in range(3):
+            eng.multiply_device(0, X.data_ptr(), Y.data_ptr(), B, stream=sp, **c)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(n):
+            eng.multiply_device(0, X.data_ptr(), Y.data_ptr(), B, stream=sp, **c)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        return a.elapsed_time(b) / n
+
+    tuning = {}
+    if args.variant == 0:
+        default_ms = timed(20, variant=3)
+        if not args.no_tune:
+            t0 = time.perf_counter()
+            eng.autotune(0, X.data_ptr(), Y.data_ptr(), B, stream=sp, reps=3)
+            tuning = {"autotune_s": round(time.perf_counter() - t0, 2),
+                      "table": [int(v) for v in eng.level_variants(0, B)]}
+        tuning["default_vps"] = B * 1000.0 / default_ms
+
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize(dev)
@@ -275,7 +298,7 @@ def main():
 
     # ---- per-launch times (same kernels, launched one by one) for the roofline
     reps = 5
-    lt = np.mean([eng.time_launches(0, X.data_ptr(), Y.data_ptr(), B, stream=sp, variant=2)
+    lt = np.mean([eng.time_launches(0, X.data_ptr(), Y.data_ptr(), B, stream=sp, variant=args.variant or 0)
                   for _ in range(reps)], axis=0)
     level_ms = float(lt[1:].sum())       # k_level launches: levels + final fold
     if args.dump_launches:
@@ -333,8 +356,10 @@ def main():
         "metric": METRIC, "value": value, "unit": "vectors/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mosaic generator + RePair)",
-        "config": workload_config(args, rows, cols) | {"variant": {1: "plain", 2: "fused", 3: "graph"}[args.variant],
-                                                      "parallelism": f"replicas x{ws}"},
+        "config": workload_config(args, rows, cols) | {
+            "variant": {0: "auto (autotuned per-launch table, CUDA graph)", 1: "plain", 2: "fused",
+                        3: "graph"}[args.variant], "parallelism": f"replicas x{ws}"},
+        "tuning": tuning,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": "k_level (all level launches of one multiply)",

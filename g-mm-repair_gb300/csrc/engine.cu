@@ -30,6 +30,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <iostream>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -483,12 +484,26 @@ static T* upload(const std::vector<T>& h, DevBuf& b) {
 }
 
 // Fully resolved launch configuration of one multiply.
+// Kernel variants a k_level launch can use: emission folding strategy and
+// chunk, and how many CTAs evaluate the level's rules (few CTAs = many
+// rules per CTA).  Variant v = emit index + GMR_N_EMIT_VARIANTS * grid index.
+struct EmitVariant {
+    int emit, chunk;
+};
+static constexpr EmitVariant kEmitVariants[] = {
+    {GMR_EMIT_SEGMENTED, 16}, {GMR_EMIT_SEGMENTED, 8}, {GMR_EMIT_SEGMENTED, 32}, {GMR_EMIT_ROWS, 0},
+    {GMR_EMIT_ATOMIC, 0}};
+static constexpr int kNumEmitVariants = 5;
+static constexpr int kOpsCtasPerSm[] = {32, 4};
+static_assert(kNumEmitVariants * 2 == GMR_N_LEVEL_VARIANTS, "variant table size");
+
 struct Launch {
     int semiring, B, Bw, VEC, G, variant, emit, chunk;
     int Bt, ntile, tile_levels;
+    std::vector<uint8_t> lv;  // per-launch variant (index = launch slot), empty = uniform emit/chunk
     bool operator==(const Launch& o) const {
         return semiring == o.semiring && B == o.B && Bw == o.Bw && VEC == o.VEC && variant == o.variant &&
-               emit == o.emit && chunk == o.chunk && Bt == o.Bt && tile_levels == o.tile_levels;
+               emit == o.emit && chunk == o.chunk && Bt == o.Bt && tile_levels == o.tile_levels && lv == o.lv;
     }
 };
 
@@ -512,6 +527,7 @@ struct gmr_engine {
     gmr::DevBuf arena, T, hX, hY;  // scratch
     cudaStream_t own_stream = nullptr;
     std::vector<gmr::GraphEntry> graphs;
+    std::map<std::pair<int, int>, std::vector<uint8_t>> level_variants;  // (semiring, B) -> per-launch variant
     int64_t last_launches = 0;
     int sm_count = 152;
     std::mutex mu;
@@ -601,7 +617,17 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
         L.em_row = static_cast<const int32_t*>(e->em_row.p);
         L.seg_row = static_cast<const int32_t*>(e->seg_row.p);
         L.seg_start = static_cast<const int64_t*>(e->seg_start.p);
-        L.em_chunk = lc.chunk;
+        const int slot = k_ops >= 1 ? k_ops : e->depth + 1;  // launch slot of this level launch
+        int emit = lc.emit, chunk = lc.chunk, ops_cap = kOpsCtasPerSm[0];
+        if (!lc.lv.empty() && slot < (int)lc.lv.size()) {
+            const int v = lc.lv[slot] % GMR_N_LEVEL_VARIANTS;
+            emit = kEmitVariants[v % kNumEmitVariants].emit;
+            chunk = kEmitVariants[v % kNumEmitVariants].chunk;
+            ops_cap = kOpsCtasPerSm[v / kNumEmitVariants];
+        }
+        if (lc.variant == GMR_VARIANT_PLAIN) emit = GMR_EMIT_ATOMIC;
+        if (chunk <= 0) chunk = 16;
+        L.em_chunk = chunk;
         int64_t nops = 0, nem = 0, nseg = 0;
         if (k_ops >= 1) {
             L.op_first = e->lvl_off[k_ops - 1];
@@ -614,24 +640,28 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
             nseg = e->seg_off[k_em + 1] - e->seg_off[k_em];
         }
         auto em_items = [&]() -> int64_t {
-            if (lc.emit == GMR_EMIT_ATOMIC) return nem * lc.G;
-            if (lc.emit == GMR_EMIT_ROWS) return nseg * lc.G;
+            if (emit == GMR_EMIT_ATOMIC) return nem * lc.G;
+            if (emit == GMR_EMIT_ROWS) return nseg * lc.G;
             if (GLOG == 0) return (nem + 1) / 2;  // two warp-blocks per warp iteration
-            return (nem + lc.chunk - 1) / lc.chunk * lc.G;
+            return (nem + chunk - 1) / chunk * lc.G;
         };
         auto go = [&](int64_t no, bool with_em) {
             LevelArgs M = L;
             M.n_ops = no;
             M.n_em = with_em ? nem : 0;
             M.n_seg = with_em ? nseg : 0;
-            if (no == 0 && M.n_em == 0) return;
+            if (no == 0 && M.n_em == 0) {
+                if (t_timer && !split) t_timer->mark();  // keep one timing slot per level launch
+                return;
+            }
             int eb = M.n_em > 0 ? blocks_for(em_items(), nt) : 0;
-            int ob = no > 0 ? blocks_for((no * lc.G + 1) / 2, nt) : 0;
+            int ob = no > 0 ? std::min<int>(blocks_for((no * lc.G + 1) / 2, nt),
+                                            std::max(1, e->sm_count * ops_cap / nt)) : 0;
             M.em_blocks = eb;
             dim3 grid(eb + ob, nt);
-            if (lc.emit == GMR_EMIT_ATOMIC)
+            if (emit == GMR_EMIT_ATOMIC)
                 k_level<S, VEC, GLOG, GMR_EMIT_ATOMIC><<<grid, TPB, 0, st>>>(s, M);
-            else if (lc.emit == GMR_EMIT_ROWS)
+            else if (emit == GMR_EMIT_ROWS)
                 k_level<S, VEC, GLOG, GMR_EMIT_ROWS><<<grid, TPB, 0, st>>>(s, M);
             else
                 k_level<S, VEC, GLOG, GMR_EMIT_SEGMENTED><<<grid, TPB, 0, st>>>(s, M);
@@ -701,8 +731,13 @@ static Launch resolve_launch(gmr_engine* e, int semiring, int B, const void* X, 
     lc.semiring = semiring;
     lc.B = B;
     lc.Bw = words_per_slot(semiring, B);
-    lc.variant = cfg && cfg->variant ? cfg->variant : GMR_VARIANT_GRAPH;
+    const int asked = cfg ? cfg->variant : GMR_VARIANT_AUTO;
+    lc.variant = asked == GMR_VARIANT_AUTO ? GMR_VARIANT_GRAPH : asked;
     if (lc.variant == GMR_VARIANT_PERSISTENT) lc.variant = GMR_VARIANT_GRAPH;  // not specialised yet
+    if (asked == GMR_VARIANT_AUTO && !(cfg && cfg->emit_mode)) {
+        auto it = e->level_variants.find({semiring, B});
+        if (it != e->level_variants.end()) lc.lv = it->second;
+    }
     lc.emit = cfg && cfg->emit_mode ? cfg->emit_mode : GMR_EMIT_SEGMENTED;
     if (lc.variant == GMR_VARIANT_PLAIN) lc.emit = GMR_EMIT_ATOMIC;
     lc.chunk = cfg && cfg->ops_per_cta > 0 ? cfg->ops_per_cta : 16;
@@ -741,12 +776,13 @@ static void ensure_scratch(gmr_engine* e, int Bw) {
 }
 
 static void multiply_device(gmr_engine* e, int semiring, const void* X, void* Y, int B, const gmr_config* cfg,
-                            cudaStream_t st) {
+                            cudaStream_t st, bool eager = false) {
     if (semiring < 0 || semiring > 2) throw Error(GMR_ERR_ARG, "unknown semiring");
     if (B < 1) throw Error(GMR_ERR_ARG, "B must be >= 1");
     if ((!X && e->cols > 0) || (!Y && e->rows > 0)) throw Error(GMR_ERR_ARG, "null X or Y");
     if (((uintptr_t)X | (uintptr_t)Y) % 4 != 0) throw Error(GMR_ERR_ARG, "X and Y must be 4-byte aligned");
     Launch lc = resolve_launch(e, semiring, B, X, Y, cfg);
+    if (eager && lc.variant == GMR_VARIANT_GRAPH) lc.variant = GMR_VARIANT_FUSED;
     ensure_scratch(e, lc.Bw);
     int64_t launches = 0;
     if (lc.variant == GMR_VARIANT_GRAPH) {
@@ -892,13 +928,11 @@ extern "C" int gmr_engine_time_launches(gmr_engine* e, int semiring, const void*
         std::lock_guard<std::mutex> lk(e->mu);
         DeviceGuard dg(e->device);
         gmr_config c = cfg ? *cfg : gmr_config{};
-        if (c.variant == GMR_VARIANT_GRAPH || c.variant == GMR_VARIANT_AUTO || c.variant == GMR_VARIANT_PERSISTENT)
-            c.variant = GMR_VARIANT_FUSED;
         LaunchTimer timer;
         timer.st = static_cast<cudaStream_t>(stream);
         t_timer = &timer;
         try {
-            multiply_device(e, semiring, dX, dY, B, &c, timer.st);
+            multiply_device(e, semiring, dX, dY, B, &c, timer.st, /*eager=*/true);
         } catch (...) {
             t_timer = nullptr;
             throw;
@@ -909,6 +943,81 @@ extern "C" int gmr_engine_time_launches(gmr_engine* e, int semiring, const void*
         if (m > cap) throw Error(GMR_ERR_RANGE, "need room for " + std::to_string(m) + " launch times");
         for (int i = 0; i < m; ++i) GMR_CUDA(cudaEventElapsedTime(&ms[i], timer.ev[i], timer.ev[i + 1]));
         *n = m;
+    });
+}
+
+extern "C" int gmr_engine_set_level_variants(gmr_engine* e, int semiring, int B, const uint8_t* v, int n) {
+    return guarded([&] {
+        if (!e) throw Error(GMR_ERR_ARG, "null engine");
+        std::lock_guard<std::mutex> lk(e->mu);
+        if (!v || n <= 0) {
+            e->level_variants.erase({semiring, B});
+            return;
+        }
+        if (n != e->depth + 2) throw Error(GMR_ERR_ARG, "need depth + 2 = " + std::to_string(e->depth + 2) + " entries");
+        for (int i = 0; i < n; ++i)
+            if (v[i] >= GMR_N_LEVEL_VARIANTS) throw Error(GMR_ERR_ARG, "variant index out of range");
+        e->level_variants[{semiring, B}] = std::vector<uint8_t>(v, v + n);
+    });
+}
+
+extern "C" int gmr_engine_get_level_variants(const gmr_engine* e, int semiring, int B, uint8_t* v, int cap,
+                                             int* n) {
+    return guarded([&] {
+        if (!e || !n) throw Error(GMR_ERR_ARG, "null argument");
+        auto* me = const_cast<gmr_engine*>(e);
+        std::lock_guard<std::mutex> lk(me->mu);
+        auto it = e->level_variants.find({semiring, B});
+        if (it == e->level_variants.end()) {
+            *n = 0;
+            return;
+        }
+        *n = (int)it->second.size();
+        if (v) {
+            if (cap < *n) throw Error(GMR_ERR_RANGE, "buffer too small");
+            std::copy(it->second.begin(), it->second.end(), v);
+        }
+    });
+}
+
+extern "C" int gmr_engine_autotune(gmr_engine* e, int semiring, const void* dX, void* dY, int B, void* stream,
+                                   int reps, float* ms, int cap) {
+    return guarded([&] {
+        if (!e) throw Error(GMR_ERR_ARG, "null engine");
+        const int nl = e->depth + 2, nv = GMR_N_LEVEL_VARIANTS;
+        if (ms && cap < nl * nv) throw Error(GMR_ERR_RANGE, "need room for (depth + 2) x variants times");
+        if (reps < 1) reps = 3;
+        std::vector<float> med((size_t)nl * nv, 0.f);
+        std::vector<uint8_t> uni(nl);
+        std::vector<float> buf((size_t)nl + 8);
+        for (int v = 0; v < nv; ++v) {
+            std::fill(uni.begin(), uni.end(), (uint8_t)v);
+            if (gmr_engine_set_level_variants(e, semiring, B, uni.data(), nl) != GMR_OK) throw Error(GMR_ERR_ARG, gmr_last_error());
+            std::vector<std::vector<float>> runs;
+            for (int r = 0; r < reps; ++r) {
+                int n = 0;
+                gmr_config c{};
+                int rc = gmr_engine_time_launches(e, semiring, dX, dY, B, &c, stream, buf.data(), (int)buf.size(), &n);
+                if (rc != GMR_OK) throw Error(rc, gmr_last_error());
+                if (n != nl) throw Error(GMR_ERR_STATE, "unexpected launch count " + std::to_string(n));
+                runs.emplace_back(buf.begin(), buf.begin() + n);
+            }
+            for (int l = 0; l < nl; ++l) {
+                std::vector<float> xs;
+                for (auto& r : runs) xs.push_back(r[l]);
+                std::nth_element(xs.begin(), xs.begin() + xs.size() / 2, xs.end());
+                med[(size_t)l * nv + v] = xs[xs.size() / 2];
+            }
+        }
+        std::vector<uint8_t> best(nl, 0);
+        for (int l = 0; l < nl; ++l) {
+            int b = 0;
+            for (int v = 1; v < nv; ++v)
+                if (med[(size_t)l * nv + v] < med[(size_t)l * nv + b]) b = v;
+            best[l] = (uint8_t)b;
+        }
+        if (gmr_engine_set_level_variants(e, semiring, B, best.data(), nl) != GMR_OK) throw Error(GMR_ERR_ARG, gmr_last_error());
+        if (ms) std::copy(med.begin(), med.end(), ms);
     });
 }
 

@@ -390,7 +390,7 @@ class Engine:
         _check(lib().gmr_engine_create(plan._h, device, C.byref(h)))
         self._h = h
         s = plan.stats
-        self.rows, self.cols = s["rows"], s["cols"]
+        self.rows, self.cols, self.depth = s["rows"], s["cols"], s["depth"]
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:
@@ -435,6 +435,32 @@ class Engine:
                                               B, C.byref(c), C.c_void_p(stream), ms.ctypes.data_as(L.F32P), cap,
                                               C.byref(n)))
         return ms[: n.value].copy()
+
+    N_LEVEL_VARIANTS = 10
+
+    def set_level_variants(self, semiring, B: int, table):
+        """Install a per-launch variant table (len depth + 2) used by AUTO multiplies; None clears."""
+        if table is None:
+            _check(lib().gmr_engine_set_level_variants(self._h, semiring_id(semiring), B, None, 0))
+            return
+        t = np.ascontiguousarray(table, dtype=np.uint8)
+        _check(lib().gmr_engine_set_level_variants(self._h, semiring_id(semiring), B,
+                                                   t.ctypes.data_as(C.POINTER(C.c_uint8)), len(t)))
+
+    def level_variants(self, semiring, B: int):
+        n = C.c_int()
+        buf = np.zeros(4096, dtype=np.uint8)
+        _check(lib().gmr_engine_get_level_variants(self._h, semiring_id(semiring), B,
+                                                   buf.ctypes.data_as(C.POINTER(C.c_uint8)), len(buf), C.byref(n)))
+        return buf[: n.value].copy() if n.value else None
+
+    def autotune(self, semiring, x_ptr: int, y_ptr: int, B: int, stream: int = 0, reps: int = 3) -> np.ndarray:
+        """Exhaustive per-launch autotuner; installs the best table and returns times[slot][variant] (ms)."""
+        depth = self.depth
+        ms = np.zeros((depth + 2) * self.N_LEVEL_VARIANTS, dtype=np.float32)
+        _check(lib().gmr_engine_autotune(self._h, semiring_id(semiring), C.c_void_p(x_ptr), C.c_void_p(y_ptr), B,
+                                         C.c_void_p(stream), reps, ms.ctypes.data_as(L.F32P), len(ms)))
+        return ms.reshape(depth + 2, self.N_LEVEL_VARIANTS)
 
     @property
     def last_launches(self) -> int:

@@ -110,6 +110,10 @@ _SIGS = {
     "gmr_engine_multiply_host": (C.c_int, [P, C.c_int, P, P, C.c_int, C.POINTER(Config)]),
     "gmr_engine_time_launches": (C.c_int, [P, C.c_int, P, P, C.c_int, C.POINTER(Config), P, F32P, C.c_int,
                                            C.POINTER(C.c_int)]),
+    "gmr_engine_set_level_variants": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(C.c_uint8), C.c_int]),
+    "gmr_engine_get_level_variants": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(C.c_uint8), C.c_int,
+                                                C.POINTER(C.c_int)]),
+    "gmr_engine_autotune": (C.c_int, [P, C.c_int, P, P, C.c_int, P, C.c_int, F32P, C.c_int]),
     "gmr_engine_last_launches": (C.c_int64, [P]),
     "gmr_engine_device_bytes": (C.c_int64, [P]),
     "gmr_engine_free": (None, [P]),

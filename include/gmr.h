@@ -252,6 +252,23 @@ int gmr_engine_multiply_host(gmr_engine* e, int semiring, const void* hX,
 int gmr_engine_time_launches(gmr_engine* e, int semiring, const void* dX, void* dY,
                              int B, const gmr_config* cfg, void* stream,
                              float* ms, int cap, int* n);
+/* Per-launch kernel variants (the autotuner's and the learned model's
+ * decision table).  Launch slot 0 is the prologue (ignored), slot k the launch
+ * of level k (rules of level k + emissions of level k-1), slot depth+1 the
+ * final fold.  Variant v = e + 5 * g: e = 0 segmented chunk 16, 1 chunk 8,
+ * 2 chunk 32 (for one lane per emission all three are the warp-shuffle
+ * reduction), 3 row-owned, 4 one atomic per emission; g = 0 up to 32 CTAs
+ * per SM evaluate the rules, g = 1 up to 4 (more rules per CTA).  An
+ * installed table is used by GMR_VARIANT_AUTO multiplies of that
+ * (semiring, B).  n = depth + 2; v = NULL clears. */
+#define GMR_N_LEVEL_VARIANTS 10
+int gmr_engine_set_level_variants(gmr_engine* e, int semiring, int B, const uint8_t* v, int n);
+int gmr_engine_get_level_variants(const gmr_engine* e, int semiring, int B, uint8_t* v, int cap, int* n);
+/* Exhaustive autotuner: times every variant on every launch (median of
+ * `reps` eager runs with the timing recorder), installs the per-launch
+ * fastest, and writes the times to ms[slot * GMR_N_LEVEL_VARIANTS + v]. */
+int gmr_engine_autotune(gmr_engine* e, int semiring, const void* dX, void* dY, int B,
+                        void* stream, int reps, float* ms, int cap);
 /* Kernel launches issued by the calling thread's last multiply. */
 int64_t gmr_engine_last_launches(const gmr_engine* e);
 /* Device bytes held by the engine (schedule + scratch). */

@@ -157,6 +157,30 @@ def test_legacy_entry_points(case, sr, monkeypatch, capfd):
     check(sr, Y, oracle_columns(s, sr, case["V"], X, rows, cols))
 
 
+@pytest.mark.parametrize("sr", range(3))
+def test_autotuned_and_mixed_tables(case, sr):
+    """Every per-launch variant table gives the same results (it only picks schedules)."""
+    torch = pytest.importorskip("torch")
+    rows, cols, B = int(case["rows"]), int(case["cols"]), 32
+    X = random_X(sr, cols, B, 77)
+    ref = oracle_columns(case["sched"], sr, case["V"], X, rows, cols)
+    eng = gmr.Engine(case["plan"])
+    Xw = engine_inputs(sr, X)
+    dX = torch.from_numpy(Xw.view(np.int32)).cuda()
+    dY = torch.empty((rows, Xw.shape[1]), dtype=torch.int32, device="cuda")
+    times = eng.autotune(sr, dX.data_ptr(), dY.data_ptr(), B)
+    assert times.shape == (eng.depth + 2, eng.N_LEVEL_VARIANTS) and np.all(times[1:] > 0)
+    best = eng.level_variants(sr, B)
+    assert best is not None and np.array_equal(best[1:], times[1:].argmin(axis=1))
+    rng = np.random.default_rng(sr)
+    for table in (best, rng.integers(0, eng.N_LEVEL_VARIANTS, eng.depth + 2)):
+        eng.set_level_variants(sr, B, table)
+        Y = engine_outputs(sr, eng.multiply(Xw, sr, B=B), B)  # AUTO uses the table
+        check(sr, Y, ref)
+    eng.set_level_variants(sr, B, None)
+    assert eng.level_variants(sr, B) is None
+
+
 def test_unittest_grammar_runlength():
     """cpu_selftest.cpp:374-467 grammar (run-length rule, coefficient 3)."""
     g = gmr.Grammar.from_arrays(5, [[1, 2], [3, 5], [6, 0], [7, 5]], [8, 0], [1.5, 2.5], kinds=[0, 0, 1, 0],
