@@ -86,6 +86,8 @@ struct gmr_plan {
     std::vector<int32_t> seg_row;             // n_seg
     std::vector<int64_t> seg_start;           // n_seg + 1
     gmr_plan_stats stats{};
+    // B-independent per-slot statistics for the cost-model features (lazy)
+    mutable std::vector<double> slot_stats;
 
     int64_t n_ops() const { return (int64_t)op_l.size(); }
     int64_t n_terms() const { return (int64_t)term_val.size() + 1; }

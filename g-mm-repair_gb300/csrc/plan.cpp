@@ -22,6 +22,7 @@
 // The reference's own layered figures (L, w*, |R|, +pt, E, E_T, U) are
 // computed alongside for reporting and for the roofline byte count.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -466,6 +467,79 @@ extern "C" int gmr_plan_from_layered(int rows, int cols, int alpha, int total_la
         s.ref_alpha = alpha;
         validate_plan(*p);
         *out = p.release();
+    });
+}
+
+
+// Per-slot statistics: [ops_k, em_{k-1}, seg_{k-1}, distinct sources_{k-1},
+// children from k-1, k-2, <= k-3, terminals] for slots k = 0 .. depth+1.
+static const std::vector<double>& slot_stats(const gmr_plan& p) {
+    if (!p.slot_stats.empty()) return p.slot_stats;
+    const int D = p.depth, NS = 8;
+    std::vector<double> st((size_t)(D + 2) * NS, 0.0);
+    std::vector<uint32_t> seen((size_t)(p.n_ops() + p.n_terms()), 0);
+    for (int k = 1; k <= D + 1; ++k) {
+        double* s = st.data() + (size_t)k * NS;
+        if (k <= D) {
+            s[0] = (double)(p.lvl_off[k] - p.lvl_off[k - 1]);
+            for (int64_t i = p.lvl_off[k - 1]; i < p.lvl_off[k]; ++i) {
+                for (int32_t c : {p.op_l[i], p.op_r[i]}) {
+                    if (c < 0) {
+                        s[7] += 1;
+                        continue;
+                    }
+                    const int lc = level_of_slot(p.lvl_off, c);
+                    const int dist = k - lc;
+                    s[dist == 1 ? 4 : (dist == 2 ? 5 : 6)] += 1;
+                }
+            }
+        }
+        const int ke = k - 1;
+        s[1] = (double)(p.em_off[ke + 1] - p.em_off[ke]);
+        s[2] = (double)(p.seg_off[ke + 1] - p.seg_off[ke]);
+        double distinct = 0;
+        for (int64_t e = p.em_off[ke]; e < p.em_off[ke + 1]; ++e) {
+            const int32_t c = p.em_src[e];
+            const size_t key = c >= 0 ? (size_t)c : (size_t)(p.n_ops() + (-(int64_t)c - 1));
+            if (seen[key] != (uint32_t)k) {
+                seen[key] = (uint32_t)k;
+                distinct += 1;
+            }
+        }
+        s[3] = distinct;
+    }
+    p.slot_stats.swap(st);
+    return p.slot_stats;
+}
+
+extern "C" int gmr_plan_launch_features(const gmr_plan* p, int semiring, int B, float* out, int cap, int* n_slots) {
+    return guarded([&] {
+        if (!p || !out || !n_slots || B < 1) throw Error(GMR_ERR_ARG, "bad argument");
+        const int D = p->depth, NF = GMR_N_BASE_FEATURES, slots = D + 2;
+        if (cap < slots * NF) throw Error(GMR_ERR_RANGE, "feature buffer too small");
+        const auto& st = slot_stats(*p);
+        const double words = semiring == GMR_BOOLEAN ? (double)((B + 31) / 32) : (double)B;
+        std::fill(out, out + (size_t)slots * NF, 0.0f);
+        for (int k = 1; k < slots; ++k) {
+            const double* s = st.data() + (size_t)k * 8;
+            float* f = out + (size_t)k * NF;
+            const double children = s[4] + s[5] + s[6] + s[7];
+            const double prev_ops = k >= 2 ? (double)(p->lvl_off[k - 1] - p->lvl_off[k - 2]) : (double)p->n_terms();
+            f[0] = (float)std::log1p(s[0]);
+            f[1] = (float)std::log1p(s[1]);
+            f[2] = (float)std::log1p(s[2]);
+            f[3] = (float)std::log1p(s[2] > 0 ? s[1] / s[2] : 0.0);
+            f[4] = (float)std::log1p(s[3] > 0 ? s[1] / s[3] : 0.0);
+            for (int j = 0; j < 4; ++j) f[5 + j] = (float)(children > 0 ? s[4 + j] / children : 0.0);
+            f[9] = (float)std::log1p(prev_ops * words * 4.0 / 1048576.0);
+            f[10] = (float)std::log2(words);
+            f[11] = semiring == GMR_BOOLEAN ? 1.0f : 0.0f;
+            f[12] = semiring == GMR_TROPICAL ? 1.0f : 0.0f;
+            f[13] = (float)std::log1p((double)p->rows);
+            f[14] = (float)std::log1p((double)p->n_ops());
+            f[15] = (float)k / (float)(D + 1);
+        }
+        *n_slots = slots;
     });
 }
 

@@ -117,6 +117,18 @@ _SIGS = {
     "gmr_engine_last_launches": (C.c_int64, [P]),
     "gmr_engine_device_bytes": (C.c_int64, [P]),
     "gmr_engine_free": (None, [P]),
+    "gmr_plan_launch_features": (C.c_int, [P, C.c_int, C.c_int, F32P, C.c_int, C.POINTER(C.c_int)]),
+    "gmr_mlp_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(P)]),
+    "gmr_mlp_info": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int64)]),
+    "gmr_mlp_params": (C.c_int, [P, F32P, F32P, C.c_int64]),
+    "gmr_mlp_set_norm": (C.c_int, [P, F32P, F32P]),
+    "gmr_mlp_predict": (C.c_int, [P, F32P, C.c_int, F32P]),
+    "gmr_mlp_gradients": (C.c_int, [P, F32P, F32P, C.c_int, F32P, C.c_int64, F32P]),
+    "gmr_mlp_train": (C.c_int, [P, F32P, F32P, C.c_int, C.c_int, C.c_int, C.c_float, C.c_uint64, F32P]),
+    "gmr_mlp_save": (C.c_int, [P, C.c_char_p]),
+    "gmr_mlp_load": (C.c_int, [C.c_char_p, C.POINTER(P)]),
+    "gmr_mlp_free": (None, [P]),
+    "gmr_engine_choose_learned": (C.c_int, [P, P, P, C.c_int, C.c_int, F32P, C.c_int]),
     "gmr_multiply_noalloc": (C.c_int, [C.POINTER(DevicePlan), C.c_int, P, P, C.c_int, P]),
     "run_gpu_right_multiply_layered": (None, [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(LayeredRule), I32P,
                                               I32P, F32P, C.c_int, F32P, C.POINTER(GPUSchedule), F32P, C.c_int]),

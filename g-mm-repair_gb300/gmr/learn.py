@@ -1,0 +1,295 @@
+"""Learned scheduler: a small MLP cost model for the per-launch kernel variant.
+
+For every launch of a multiply (the launch of level k: rules of level k and
+emissions of level k-1) the engine can run any of GMR_N_LEVEL_VARIANTS kernel
+variants (emission folding strategy x rules-per-CTA grid).  The exhaustive
+autotuner (gmr_engine_autotune) measures all of them with the timing
+recorder; this module turns those measurements into training data, trains a
+3 x 64 fp32 MLP on the GPU with the library's own forward/backward/Adam
+kernels, and uses it (gmr_engine_choose_learned, an inference kernel) to pick
+the variants without measuring.  When no model is available the measured
+autotuner choice is used; the autotuner also judges the model's regret.  The
+model only picks schedules: every variant computes the same Y.
+
+    python -m gmr.learn --out DIR [--grammars N]   # record, train, evaluate (GPU)
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import time
+from pathlib import Path
+
+import numpy as np
+
+from . import _lib as L
+from . import Engine, Grammar, Plan, _check, gen_copy_graph, gen_mosaic, lib, repair, semiring_id
+
+N_BASE = 16
+N_VAR = 10
+IN_DIM = N_BASE + N_VAR
+MODEL_PATH = Path(__file__).resolve().parent / "models" / "cost_model.gmrmlp"
+
+
+def launch_features(plan: Plan, semiring, B: int) -> np.ndarray:
+    """[depth + 2][16] base features of every launch slot (slot 0 = prologue, zeros)."""
+    d = plan.stats["depth"]
+    out = np.zeros((d + 2) * N_BASE, dtype=np.float32)
+    n = C.c_int()
+    _check(lib().gmr_plan_launch_features(plan._h, semiring_id(semiring), B, out.ctypes.data_as(L.F32P), len(out),
+                                          C.byref(n)))
+    return out.reshape(n.value, N_BASE)
+
+
+def model_inputs(base: np.ndarray) -> np.ndarray:
+    """[slots][16] -> [slots * N_VAR][26]: base features + variant one-hot."""
+    slots = base.shape[0]
+    X = np.zeros((slots, N_VAR, IN_DIM), dtype=np.float32)
+    X[:, :, :N_BASE] = base[:, None, :]
+    X[:, np.arange(N_VAR), N_BASE + np.arange(N_VAR)] = 1.0
+    return X.reshape(slots * N_VAR, IN_DIM)
+
+
+class Mlp:
+    """The cost model (libgmr's gmr_mlp): in -> 64 -> 64 -> 64 -> 1, ReLU, fp32."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    @classmethod
+    def create(cls, in_dim=IN_DIM, hidden=64, layers=3, seed=0) -> "Mlp":
+        h = C.c_void_p()
+        _check(lib().gmr_mlp_create(in_dim, hidden, layers, seed, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def load(cls, path=MODEL_PATH) -> "Mlp":
+        h = C.c_void_p()
+        _check(lib().gmr_mlp_load(os.fsencode(str(path)), C.byref(h)))
+        return cls(h)
+
+    def save(self, path):
+        _check(lib().gmr_mlp_save(self._h, os.fsencode(str(path))))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().gmr_mlp_free(self._h)
+            self._h = C.c_void_p()
+
+    @property
+    def n_params(self) -> int:
+        n = C.c_int64()
+        _check(lib().gmr_mlp_info(self._h, None, None, None, C.byref(n)))
+        return n.value
+
+    def params(self) -> np.ndarray:
+        p = np.zeros(self.n_params, dtype=np.float32)
+        _check(lib().gmr_mlp_params(self._h, p.ctypes.data_as(L.F32P), None, len(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        _check(lib().gmr_mlp_params(self._h, None, p.ctypes.data_as(L.F32P), len(p)))
+
+    def set_norm(self, mean, std):
+        mean = np.ascontiguousarray(mean, dtype=np.float32)
+        std = np.ascontiguousarray(std, dtype=np.float32)
+        _check(lib().gmr_mlp_set_norm(self._h, mean.ctypes.data_as(L.F32P), std.ctypes.data_as(L.F32P)))
+
+    def predict(self, X) -> np.ndarray:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.zeros(len(X), dtype=np.float32)
+        _check(lib().gmr_mlp_predict(self._h, X.ctypes.data_as(L.F32P), len(X), Y.ctypes.data_as(L.F32P)))
+        return Y
+
+    def gradients(self, X, T):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        g = np.zeros(self.n_params, dtype=np.float32)
+        loss = C.c_float()
+        _check(lib().gmr_mlp_gradients(self._h, X.ctypes.data_as(L.F32P), T.ctypes.data_as(L.F32P), len(X),
+                                       g.ctypes.data_as(L.F32P), len(g), C.byref(loss)))
+        return g, float(loss.value)
+
+    def train(self, X, T, epochs=60, batch=512, lr=2e-3, seed=0) -> float:
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        loss = C.c_float()
+        _check(lib().gmr_mlp_train(self._h, X.ctypes.data_as(L.F32P), T.ctypes.data_as(L.F32P), len(X), epochs,
+                                   batch, lr, seed, C.byref(loss)))
+        return float(loss.value)
+
+
+def choose_learned(eng: Engine, plan: Plan, model: Mlp, semiring, B: int) -> np.ndarray:
+    """Installs the model's per-launch choice; returns its predictions [slots][variants] (log us)."""
+    slots = plan.stats["depth"] + 2
+    pred = np.zeros(slots * N_VAR, dtype=np.float32)
+    _check(lib().gmr_engine_choose_learned(eng._h, plan._h, model._h, semiring_id(semiring), B,
+                                           pred.ctypes.data_as(L.F32P), len(pred)))
+    return pred.reshape(slots, N_VAR)
+
+
+# ---------------------------------------------------------------- corpus
+def corpus_specs(n_mosaic: int, n_graph: int, seed0: int = 100):
+    """Seeded grammar specs over the scheduler corpus ranges, scaled to fit one
+    GPU session: mosaics (rows 10k-60k, cols 1k-10k, founders 16-1024,
+    switch rate 1e-3 to 5e-2) and copy-model graphs (nodes 0.2M-1.5M,
+    degree 8-32, copy probability 0.3-0.9)."""
+    specs = []
+    for i in range(n_mosaic):
+        r = np.random.default_rng(seed0 + i)
+        specs.append(dict(kind="mosaic", seed=seed0 + i, rows=int(r.integers(10_000, 60_001)),
+                          cols=int(r.integers(1_000, 10_001)), founders=int(2 ** r.uniform(4, 10)),
+                          switch=float(10 ** r.uniform(-3, np.log10(5e-2))), mutation=1e-3))
+    for i in range(n_graph):
+        r = np.random.default_rng(seed0 + 1000 + i)
+        specs.append(dict(kind="graph", seed=seed0 + 1000 + i, nodes=int(r.integers(200_000, 1_500_001)),
+                          degree=int(r.integers(8, 33)), copy=float(r.uniform(0.3, 0.9))))
+    return specs
+
+
+def make_grammar(spec, threads=0):
+    if spec["kind"] == "mosaic":
+        m = gen_mosaic(spec["rows"], spec["cols"], spec["founders"], spec["switch"], spec["mutation"], spec["seed"],
+                       threads)
+        return repair(m, threads), spec["rows"], spec["cols"]
+    m = gen_copy_graph(spec["nodes"], spec["degree"], spec["copy"], True, spec["seed"], threads)
+    return repair(m, threads), spec["nodes"], spec["nodes"]
+
+
+def random_inputs(torch, semiring: int, cols: int, B: int, seed: int):
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    if semiring == 0:
+        X = torch.rand((cols, B), device="cuda", generator=g) * 2 - 1
+        return X, B
+    if semiring == 1:
+        W = (B + 31) // 32
+        X = torch.randint(0, 2**31 - 1, (cols, W), device="cuda", generator=g, dtype=torch.int32)
+        return X, W
+    X = torch.randint(0, 1000, (cols, B), device="cuda", generator=g, dtype=torch.int32)
+    return X, B
+
+
+def record(eng: Engine, plan: Plan, semiring: int, B: int, seed: int, reps: int = 3):
+    """Autotuner timings of every (launch, variant) -> (inputs [slots*V][26], log us [slots*V], times [slots][V])."""
+    import torch
+
+    X, words = random_inputs(torch, semiring, eng.cols, B, seed)
+    Y = torch.empty((eng.rows, words), device="cuda", dtype=X.dtype)
+    stream = torch.cuda.current_stream().cuda_stream
+    times = eng.autotune(semiring, X.data_ptr(), Y.data_ptr(), B, stream=stream, reps=reps)
+    base = launch_features(plan, semiring, B)
+    Xin = model_inputs(base)
+    T = np.log(np.maximum(times.reshape(-1), 1e-4) * 1000.0).astype(np.float32)  # ms -> log us
+    keep = np.repeat(np.arange(base.shape[0]) >= 1, N_VAR)  # drop the prologue slot
+    return Xin[keep], T[keep], times
+
+
+def sweep_time(eng: Engine, semiring: int, B: int, table, seed: int, n: int = 10) -> float:
+    """Device time (ms) of one AUTO multiply (CUDA graph) with `table` installed."""
+    import torch
+
+    X, words = random_inputs(torch, semiring, eng.cols, B, seed)
+    Y = torch.empty((eng.rows, words), device="cuda", dtype=X.dtype)
+    st = torch.cuda.current_stream()
+    eng.set_level_variants(semiring, B, table)
+    for _ in range(3):
+        eng.multiply_device(semiring, X.data_ptr(), Y.data_ptr(), B, stream=st.cuda_stream)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    for _ in range(n):
+        eng.multiply_device(semiring, X.data_ptr(), Y.data_ptr(), B, stream=st.cuda_stream)
+    b.record(st)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / n
+
+
+def plain_time(eng: Engine, semiring: int, B: int, seed: int, n: int = 5) -> float:
+    import torch
+
+    X, words = random_inputs(torch, semiring, eng.cols, B, seed)
+    Y = torch.empty((eng.rows, words), device="cuda", dtype=X.dtype)
+    st = torch.cuda.current_stream()
+    for _ in range(2):
+        eng.multiply_device(semiring, X.data_ptr(), Y.data_ptr(), B, stream=st.cuda_stream, variant=1)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(st)
+    for _ in range(n):
+        eng.multiply_device(semiring, X.data_ptr(), Y.data_ptr(), B, stream=st.cuda_stream, variant=1)
+    b.record(st)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / n
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", required=True)
+    ap.add_argument("--mosaic", type=int, default=36)
+    ap.add_argument("--graph", type=int, default=12)
+    ap.add_argument("--holdout", type=float, default=0.25)
+    ap.add_argument("--Bs", default="1,8,32,128")
+    ap.add_argument("--epochs", type=int, default=80)
+    args = ap.parse_args()
+    out = Path(args.out)
+    out.mkdir(parents=True, exist_ok=True)
+    Bs = [int(b) for b in args.Bs.split(",")]
+    specs = corpus_specs(args.mosaic, args.graph)
+    rng = np.random.default_rng(7)
+    order = rng.permutation(len(specs))
+    n_hold = int(round(len(specs) * args.holdout))
+    hold = set(order[:n_hold].tolist())
+    rows_tr, rows_te = [], []
+    t0 = time.time()
+    for gi, spec in enumerate(specs):
+        g, rows, cols = make_grammar(spec)
+        plan = Plan.build(g, rows, cols)
+        eng = Engine(plan)
+        for sr in (0, 1, 2):
+            for B in Bs:
+                seed = 1000 * gi + 10 * sr + B
+                Xin, T, times = record(eng, plan, sr, B, seed)
+                rec = dict(g=gi, sr=sr, B=B, X=Xin, T=T, times=times, ops=plan.stats["n_ops"])
+                (rows_te if gi in hold else rows_tr).append(rec)
+        print(json.dumps(dict(grammar=gi, spec=spec, ops=plan.stats["n_ops"], depth=plan.stats["depth"],
+                              held_out=gi in hold, elapsed_s=round(time.time() - t0, 1))), flush=True)
+        del eng
+    Xtr = np.concatenate([r["X"] for r in rows_tr])
+    Ttr = np.concatenate([r["T"] for r in rows_tr])
+    np.savez_compressed(out / "dataset.npz", Xtr=Xtr, Ttr=Ttr, Xte=np.concatenate([r["X"] for r in rows_te]),
+                        Tte=np.concatenate([r["T"] for r in rows_te]))
+    model = Mlp.create(seed=1)
+    mean, std = Xtr.mean(axis=0), Xtr.std(axis=0)
+    std[std < 1e-6] = 1.0
+    model.set_norm(mean, std)
+    t1 = time.time()
+    loss = model.train(Xtr, Ttr, epochs=args.epochs, batch=512, lr=2e-3, seed=3)
+    train_s = time.time() - t1
+    model.save(out / "cost_model.gmrmlp")
+    # held-out regret: predicted choice vs measured best, on the measured times
+    regrets, default_gain, wins = [], [], 0
+    for r in rows_te:
+        times = r["times"][1:]                      # [slots-1][V] ms
+        pred = model.predict(r["X"]).reshape(times.shape)
+        pick = pred.argmin(axis=1)
+        t_learn = times[np.arange(len(pick)), pick].sum()
+        t_best = times.min(axis=1).sum()
+        t_default = times[:, 0].sum()
+        regrets.append(t_learn / t_best - 1.0)
+        default_gain.append(t_default / t_learn)
+        wins += t_learn <= t_default
+    te_loss = float(np.mean((model.predict(np.concatenate([r["X"] for r in rows_te])) -
+                             np.concatenate([r["T"] for r in rows_te])) ** 2))
+    report = dict(grammars=len(specs), train_grammars=len(specs) - n_hold, heldout_grammars=n_hold,
+                  train_rows=int(len(Xtr)), train_mse=loss, heldout_mse=te_loss, train_s=round(train_s, 2),
+                  regret_mean=float(np.mean(regrets)), regret_median=float(np.median(regrets)),
+                  regret_p90=float(np.percentile(regrets, 90)), within_10pct=float(np.mean(np.array(regrets) <= 0.10)),
+                  gain_vs_default_mean=float(np.mean(default_gain)), learned_not_slower_than_default=wins / len(rows_te),
+                  cases=len(rows_te), record_s=round(t1 - t0, 1))
+    (out / "report.json").write_text(json.dumps(report, indent=1))
+    print(json.dumps(report), flush=True)
+
+
+if __name__ == "__main__":
+    main()

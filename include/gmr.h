@@ -269,6 +269,49 @@ int gmr_engine_get_level_variants(const gmr_engine* e, int semiring, int B, uint
  * fastest, and writes the times to ms[slot * GMR_N_LEVEL_VARIANTS + v]. */
 int gmr_engine_autotune(gmr_engine* e, int semiring, const void* dX, void* dY, int B,
                         void* stream, int reps, float* ms, int cap);
+/* ------------------------------------------------------------------ */
+/* Learned cost model for the per-launch variant choice                */
+/* ------------------------------------------------------------------ */
+/* Features of each launch slot (depth + 2 slots, slot 0 all zero):
+ *  0 log1p rules of level k          1 log1p emissions of level k-1
+ *  2 log1p row segments of level k-1 3 log1p emissions per segment
+ *  4 log1p emissions per distinct source (fan-out)
+ *  5..8 fraction of the level's child references from level k-1, k-2,
+ *       <= k-3, terminals (child-distance histogram)
+ *  9 log1p MB of level k-1 values at this B   10 log2 words per slot
+ * 11 semiring is (OR,AND)   12 semiring is (min,+)   13 log1p rows
+ * 14 log1p rules in total   15 k / (depth + 1)
+ * out: [slots][GMR_N_BASE_FEATURES]. */
+#define GMR_N_BASE_FEATURES 16
+int gmr_plan_launch_features(const gmr_plan* p, int semiring, int B, float* out, int cap, int* n_slots);
+
+/* Fully connected ReLU network in -> hidden^layers -> 1 (fp32), trained and
+ * evaluated by this library's CUDA kernels.  Input rows are the base
+ * features followed by a one-hot of the variant (in = GMR_N_BASE_FEATURES +
+ * GMR_N_LEVEL_VARIANTS); the target is log(launch time in microseconds). */
+typedef struct gmr_mlp gmr_mlp;
+int gmr_mlp_create(int in_dim, int hidden, int layers, uint64_t seed, gmr_mlp** out);
+int gmr_mlp_info(const gmr_mlp* m, int* in_dim, int* hidden, int* layers, int64_t* n_params);
+/* get / set the flat parameter vector [W1 b1 W2 b2 ... Wout bout] (either may be NULL) */
+int gmr_mlp_params(gmr_mlp* m, float* get, const float* set, int64_t n);
+/* input normalisation: x' = (x - mean) / std */
+int gmr_mlp_set_norm(gmr_mlp* m, const float* mean, const float* std);
+int gmr_mlp_predict(const gmr_mlp* m, const float* X, int N, float* Y);
+/* gradient of the mean squared error over the N rows (one forward + backward) */
+int gmr_mlp_gradients(gmr_mlp* m, const float* X, const float* T, int N, float* grad, int64_t n, float* loss);
+/* Adam, mini-batches of `batch` rows, `epochs` passes; final full-data MSE to *loss */
+int gmr_mlp_train(gmr_mlp* m, const float* X, const float* T, int N, int epochs, int batch, float lr,
+                  uint64_t seed, float* loss);
+/* versioned ("GMRMLP01") file with a CRC-32 of its contents */
+int gmr_mlp_save(const gmr_mlp* m, const char* path);
+int gmr_mlp_load(const char* path, gmr_mlp** out);
+void gmr_mlp_free(gmr_mlp* m);
+/* Predicts every variant's time on every launch of (semiring, B), installs
+ * the per-launch argmin as the engine's table, writes the predictions (log us)
+ * to pred[slot * GMR_N_LEVEL_VARIANTS + v] when pred != NULL. */
+int gmr_engine_choose_learned(gmr_engine* e, const gmr_plan* p, const gmr_mlp* m, int semiring, int B,
+                              float* pred, int cap);
+
 /* Kernel launches issued by the calling thread's last multiply. */
 int64_t gmr_engine_last_launches(const gmr_engine* e);
 /* Device bytes held by the engine (schedule + scratch). */
