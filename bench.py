@@ -6,9 +6,17 @@ switch rate 0.005, mutation 5e-4, seed 2), RePair-compressed by this
 project's compressor, times X of 10,000 x 32 fp32 ~ U[-1,1] ((+,x) semiring).
 A step is one multiply of all 32 right-hand sides.  Inputs are synthetic and
 seeded; the grammar (about 1 GB of rules and emissions) is larger than the
-129 MB L2, so no extra L2 flush is done between steps.
+129 MB L2, so no extra L2 flush is done between steps.  The headline uses the
+learned per-launch kernel choice (the committed cost model) and reports the
+exhaustive autotuner's choice and the untuned engine beside it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gmr|reference]
+                    [--workload NAME] [--semiring S] [--B B]
+
+Other workloads (not the headline): mosaic-20000x5000 (the CPU-runnable size),
+graph-16777216 (copy-model graph, 16.8M nodes, degree 24; --semiring boolean
+with B = 32 bit-packed frontiers, or tropical) and pack8 (eight uneven mosaic
+grammars, each with its own B, in one graph launch).
 
 --impl reference times the reference's CPU implementation of the path (the
 OpenMP level sweep of gpu_engine_test.cu:49-104, as restated in oracle/) on the
@@ -34,11 +42,15 @@ sys.path.insert(0, str(REPO / "g-mm-repair_gb300"))
 sys.path.insert(0, str(REPO))
 
 METRIC = "vectors/s & %HBM roofline, batched+learned vs plain sweep on GB300 (rel err≤1e-5)"
-WORKLOADS = {
+MOSAICS = {
     # name: rows, cols, founders, switch, mutation, seed
     "mosaic-200000x10000": (200_000, 10_000, 256, 0.005, 5e-4, 2),
     "mosaic-20000x5000": (20_000, 5_000, 64, 0.01, 1e-3, 0),
 }
+GRAPH = (16_777_216, 24, 0.7, 3)  # nodes, mean out-degree, copy probability, seed
+WORKLOADS = list(MOSAICS) + ["graph-16777216", "pack8"]
+SR_IDS = {"plustimes": 0, "boolean": 1, "tropical": 2}
+INT_MAX = 2**31 - 1
 
 
 def log(*a):
@@ -52,29 +64,84 @@ def dist_env():
     return ws, rank, local
 
 
-def load_or_make_grammar(name: str, threads: int = 0):
+def cache_dir() -> Path:
+    d = Path(os.environ.get("GMR_CACHE_DIR", REPO / "_cache"))
+    d.mkdir(parents=True, exist_ok=True)
+    return d
+
+
+def cached_grammar(key: str, make):
+    """Grammar from the cache directory, or make() -> (grammar, info) and store it."""
     import gmr
 
-    rows, cols, F, sw, mu, seed = WORKLOADS[name]
-    cache = Path(os.environ.get("GMR_CACHE_DIR", REPO / "_cache"))
-    cache.mkdir(parents=True, exist_ok=True)
-    base = cache / f"{name}-s{seed}"
+    base = cache_dir() / key
     if Path(str(base) + ".vc.R").exists():
-        return gmr.Grammar.load(base), rows, cols, {"cached": True}
-    t0 = time.perf_counter()
-    m = gmr.gen_mosaic(rows, cols, F, sw, mu, seed, threads)
-    nnz = m.nnz
-    t1 = time.perf_counter()
-    g = gmr.repair(m, threads)
-    t2 = time.perf_counter()
-    del m
+        return gmr.Grammar.load(base), {"cached": True}
+    g, info = make()
     tmp = Path(str(base) + ".tmp")
     g.save(tmp)
     for ext in (".vc.R", ".vc.C", ".val"):
         os.replace(str(tmp) + ext, str(base) + ext)
-    log(f"grammar {name}: nnz={nnz} gen {t1 - t0:.1f}s repair {t2 - t1:.1f}s")
-    return g, rows, cols, {"cached": False, "nnz": int(nnz), "gen_s": round(t1 - t0, 2),
-                           "repair_s": round(t2 - t1, 2)}
+    return g, info | {"cached": False}
+
+
+def mosaic_grammar(rows, cols, F, sw, mu, seed):
+    import gmr
+
+    def make():
+        t0 = time.perf_counter()
+        m = gmr.gen_mosaic(rows, cols, F, sw, mu, seed)
+        t1 = time.perf_counter()
+        g = gmr.repair(m)
+        t2 = time.perf_counter()
+        log(f"grammar mosaic {rows}x{cols}: nnz={m.nnz} gen {t1 - t0:.1f}s repair {t2 - t1:.1f}s")
+        return g, {"nnz": int(m.nnz), "gen_s": round(t1 - t0, 2), "repair_s": round(t2 - t1, 2)}
+
+    return cached_grammar(f"mosaic-{rows}x{cols}-f{F}-s{seed}", make)
+
+
+def graph_grammar(weighted: bool):
+    import gmr
+
+    nodes, deg, cp, seed = GRAPH
+
+    def make():
+        t0 = time.perf_counter()
+        m = gmr.gen_copy_graph(nodes, deg, cp, weighted, seed)
+        t1 = time.perf_counter()
+        g = gmr.repair(m)
+        t2 = time.perf_counter()
+        log(f"grammar graph {nodes}: nnz={m.nnz} gen {t1 - t0:.1f}s repair {t2 - t1:.1f}s")
+        return g, {"nnz": int(m.nnz), "gen_s": round(t1 - t0, 2), "repair_s": round(t2 - t1, 2)}
+
+    return cached_grammar(f"graph-{nodes}-d{deg}-w{int(weighted)}-s{seed}", make)
+
+
+def workload_grammar(args):
+    if args.workload in MOSAICS:
+        rows, cols, F, sw, mu, seed = MOSAICS[args.workload]
+        g, info = mosaic_grammar(rows, cols, F, sw, mu, seed)
+        return g, rows, cols, info
+    g, info = graph_grammar(args.semiring == "tropical")
+    return g, GRAPH[0], GRAPH[0], info
+
+
+def make_inputs(sr: int, cols: int, B: int, seed: int):
+    """Host inputs in the engine's element type: fp32 U[-1,1]; bit-packed 1 %-dense
+    frontiers; int32 with 99 % INT_MAX (+inf) and 1 % U{0..1000}."""
+    rng = np.random.default_rng(seed)
+    if sr == 0:
+        return rng.uniform(-1, 1, (cols, B)).astype(np.float32)
+    if sr == 1:
+        W = (B + 31) // 32
+        bits = rng.random((cols, W * 32)) < 0.01
+        bits[:, B:] = False
+        words = (bits.reshape(cols, W, 32).astype(np.uint64) << np.arange(32, dtype=np.uint64)).sum(axis=2)
+        return words.astype(np.uint32)
+    X = np.full((cols, B), INT_MAX, dtype=np.int32)
+    hot = rng.random((cols, B)) < 0.01
+    X[hot] = rng.integers(0, 1001, int(hot.sum()))
+    return X
 
 
 class ClockSampler:
@@ -135,8 +202,20 @@ def measured_peak_hbm():
     return 6800.0, "fallback"
 
 
-def cpu_reference_rate(g, rows, cols, seconds: float, threads: int, gpu_y0=None, x0=None):
-    """The reference's OpenMP CPU sweep (oracle restatement), on the host cores."""
+def oracle_x(sr: int, Xh: np.ndarray, col: int) -> np.ndarray:
+    """Column `col` of the inputs as the reference's float x."""
+    if sr == 0:
+        return Xh[:, col].astype(np.float32)
+    if sr == 1:
+        return ((Xh[:, col // 32] >> np.uint32(col % 32)) & 1).astype(np.float32)
+    x = Xh[:, col].astype(np.float64)
+    x[x >= 1e9] = 1e9
+    return x.astype(np.float32)
+
+
+def cpu_reference_rate(g, sr, rows, cols, seconds: float, threads: int, gpu_y0=None, x0=None):
+    """The reference's OpenMP CPU sweep (oracle restatement), on the host cores;
+    also checks the GPU's first column against the oracle."""
     from oracle import oracle as O
 
     t0 = time.perf_counter()
@@ -144,36 +223,60 @@ def cpu_reference_rate(g, rows, cols, seconds: float, threads: int, gpu_y0=None,
     build_s = time.perf_counter() - t0
     V = g.values().astype(np.float32)
     rng = np.random.default_rng(1)
-    n, spent, err = 0, 0.0, None
+    n, spent, check = 0, 0.0, None
     while n < 1 or (spent < seconds and n < 20):
         x = x0 if (n == 0 and x0 is not None) else rng.uniform(-1, 1, cols).astype(np.float32)
         t = time.perf_counter()
-        sched.cpu_reference(0, V, x, rows, cols, threads=threads)
+        y_cpu = sched.cpu_reference(sr, V, x, rows, cols, threads=threads)
         spent += time.perf_counter() - t
+        if n == 0 and gpu_y0 is not None and x0 is not None:
+            if sr == 0:
+                y64 = sched.sweep_f64(0, V.astype(np.float64), x0, rows, cols)
+                check = {"rel_err_fp64": float(np.abs(gpu_y0.astype(np.float64) - y64).max() /
+                                                max(np.abs(y64).max(), 1e-30))}
+            else:
+                check = {"mismatches_vs_reference_sweep": int(np.sum(gpu_y0.astype(np.int64) != y_cpu))}
         n += 1
-    if gpu_y0 is not None and x0 is not None:
-        y64 = sched.sweep_f64(0, V.astype(np.float64), x0, rows, cols)
-        err = float(np.abs(gpu_y0.astype(np.float64) - y64).max() / max(np.abs(y64).max(), 1e-30))
-    return n / spent, n, spent, build_s, err
+    return n / spent, n, spent, build_s, check
+
+
+def dtype_of(sr):
+    return {0: "f32", 1: "u32 (32 bit-packed OR-AND vectors)", 2: "i32"}[sr]
+
+
+def workload_config(args, rows, cols):
+    cfg = {"workload": args.workload, "semiring": args.semiring, "B": args.B, "rows": rows, "cols": cols,
+           "l2": "inputs larger than L2 (grammar streams > 129 MB each step); no flush"}
+    if args.workload in MOSAICS:
+        r, c, F, sw, mu, seed = MOSAICS[args.workload]
+        cfg |= {"kind": "mosaic genotype RePair grammar", "founders": F, "switch_rate": sw, "mutation": mu,
+                "seed": seed, "x": "fp32 U[-1,1]" if args.semiring == "plustimes" else args.semiring}
+    elif args.workload == "graph-16777216":
+        cfg |= {"kind": "copy-model graph RePair grammar", "degree": GRAPH[1], "copy_prob": GRAPH[2],
+                "seed": GRAPH[3]}
+    return cfg
 
 
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    g, rows, cols, _ = load_or_make_grammar(args.workload)
+    if args.workload == "pack8":
+        print(json.dumps({"impl": "reference", "unavailable": "pack8 has no single-grammar CPU path"}))
+        return 0
+    g, rows, cols, _ = workload_grammar(args)
     threads = os.cpu_count() or 1
+    sr = SR_IDS[args.semiring]
     per_step = []
     for _ in range(args.warmup + args.steps):
-        rate, n, spent, build_s, _ = cpu_reference_rate(g, rows, cols, args.ref_seconds, threads)
+        rate, n, spent, build_s, _ = cpu_reference_rate(g, sr, rows, cols, args.ref_seconds, threads)
         per_step.append(rate)
-    vals = per_step[args.warmup:]
-    v = statistics.median(vals)
-    cfg = workload_config(args, rows, cols)
+    v = statistics.median(per_step[args.warmup:])
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "vectors/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
+        "scaling": "weak", "vs_baseline": None, "dtype": dtype_of(sr), "data": "synthetic",
+        "config": workload_config(args, rows, cols),
         "cpu_baseline": {"value": v, "unit": "vectors/s", "cores": threads, "kind": "port",
                          "sample": f"each step: the reference's OpenMP layered CPU sweep (restated in oracle/) on "
                                    f"1-20 single vectors of the same grammar for ~{args.ref_seconds:.0f} s; "
@@ -184,12 +287,72 @@ def run_reference(args):
     return 0
 
 
-def workload_config(args, rows, cols):
-    r, c, F, sw, mu, seed = WORKLOADS[args.workload]
-    return {"workload": f"{args.workload} mosaic genotype RePair grammar x X[{cols}x{args.B}] fp32 U[-1,1]",
-            "rows": rows, "cols": cols, "founders": F, "switch_rate": sw, "mutation": mu, "seed": seed,
-            "B": args.B, "semiring": "plustimes",
-            "l2": "inputs larger than L2 (grammar streams > 129 MB each step); no flush"}
+def timed_loop(torch, stream, fn, n):
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(n):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / n
+
+
+def run_pack8(args):
+    """Eight mosaic grammars of uneven size (rows ~U{5k..200k}, cols ~U{1k..10k},
+    seeds 10-17), each with its own B in {1, 4, 16, 64}, in one graph launch."""
+    import torch
+
+    import gmr
+
+    rng = np.random.default_rng(17)
+    engines, Xs, Ys, Bs, total_alg, info = [], [], [], [], 0.0, []
+    for i in range(8):
+        rows, cols = int(rng.integers(5_000, 200_001)), int(rng.integers(1_000, 10_001))
+        g, gi = mosaic_grammar(rows, cols, 64, 0.01, 1e-3, 10 + i)
+        plan = gmr.Plan.build(g, rows, cols)
+        B = [1, 4, 16, 64][i % 4]
+        eng = gmr.Engine(plan)
+        X = torch.from_numpy(make_inputs(0, cols, B, 100 + i)).cuda()
+        Y = torch.empty((rows, B), device="cuda")
+        st = torch.cuda.current_stream().cuda_stream
+        eng.autotune(0, X.data_ptr(), Y.data_ptr(), B, stream=st)
+        engines.append(eng)
+        Xs.append(X)
+        Ys.append(Y)
+        Bs.append(B)
+        total_alg += plan.alg_bytes(0, B)
+        info.append({"rows": rows, "cols": cols, "B": B, "ops": plan.stats["n_ops"]})
+    pack = gmr.Pack(engines)
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    def packed():
+        pack.multiply_device([0] * 8, [x.data_ptr() for x in Xs], [y.data_ptr() for y in Ys], Bs, stream=sp)
+
+    def sequential():
+        for e, x, y, b in zip(engines, Xs, Ys, Bs):
+            e.multiply_device(0, x.data_ptr(), y.data_ptr(), b, stream=sp)
+
+    for _ in range(args.warmup):
+        packed()
+        sequential()
+    ms_seq = timed_loop(torch, stream, sequential, args.steps)
+    sampler = ClockSampler(0)
+    sampler.start()
+    time.sleep(0.3)
+    ms = timed_loop(torch, stream, packed, args.steps)
+    clocks = sampler.stop()
+    vecs = sum(Bs)
+    out = {"metric": METRIC, "value": vecs * 1000.0 / ms, "unit": "vectors/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "pack8", "grammars": info, "seeds": list(range(10, 18)),
+                      "l2": "inputs larger than L2; no flush"},
+           "sequential_vps": vecs * 1000.0 / ms_seq, "pack_gain": ms_seq / ms,
+           "step_alg_gbs": total_alg / (ms / 1000.0) / 1e9, "gpu_launches": int(pack.last_launches * args.steps),
+           "clocks": clocks}
+    print(json.dumps(out), flush=True)
+    return 0
 
 
 def main():
@@ -198,23 +361,30 @@ def main():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gmr", "reference"], default="gmr")
-    ap.add_argument("--workload", choices=list(WORKLOADS), default="mosaic-200000x10000")
+    ap.add_argument("--workload", choices=WORKLOADS, default="mosaic-200000x10000")
+    ap.add_argument("--semiring", choices=list(SR_IDS), default=None)
     ap.add_argument("--B", type=int, default=32)
     ap.add_argument("--variant", type=int, default=0,
-                    help="0 auto (autotuned per-launch table, CUDA graph), 1 plain, 2 fused, 3 graph")
-    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (AUTO = engine defaults)")
+                    help="0 auto (learned / autotuned per-launch table, CUDA graph), 1 plain, 2 fused, 3 graph, "
+                         "4 persistent")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner and the learned choice")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-seconds", type=float, default=6.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--dump-launches", action="store_true", help="per-launch times and level sizes to stderr")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.semiring is None:
+        args.semiring = "boolean" if args.workload == "graph-16777216" else "plustimes"
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "pack8":
+        return run_pack8(args)
 
     import torch
 
     import gmr
+    from gmr import learn
 
     ws, rank, local = dist_env()
     if ws > 1:
@@ -226,7 +396,7 @@ def main():
 
     if ws > 1 and rank != 0:
         torch.distributed.barrier()
-    g, rows, cols, ginfo = load_or_make_grammar(args.workload)
+    g, rows, cols, ginfo = workload_grammar(args)
     if ws > 1 and rank == 0:
         torch.distributed.barrier()
     t0 = time.perf_counter()
@@ -234,38 +404,47 @@ def main():
     plan_s = time.perf_counter() - t0
     st = plan.stats
     eng = gmr.Engine(plan, device=local)
+    sr = SR_IDS[args.semiring]
     B = args.B
-    rng = np.random.default_rng(1 + rank)
-    Xh = rng.uniform(-1, 1, (cols, B)).astype(np.float32)
-    X = torch.from_numpy(Xh).to(dev)
-    Y = torch.empty((rows, B), dtype=torch.float32, device=dev)
+    Xh = make_inputs(sr, cols, B, 1 + rank)
+    words = Xh.shape[1]
+    X = torch.from_numpy(Xh.view(np.int32)).to(dev)
+    Y = torch.empty((rows, words), dtype=torch.int32, device=dev)
     stream = torch.cuda.current_stream(dev)
     sp = stream.cuda_stream
     cfg = dict(variant=args.variant)
 
     def step():
-        eng.multiply_device(0, X.data_ptr(), Y.data_ptr(), B, stream=sp, **cfg)
+        eng.multiply_device(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, **cfg)
 
     def timed(n, **c):
         for _ in range(3):
-            eng.multiply_device(0, X.data_ptr(), Y.data_ptr(), B, stream=sp, **c)
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        for _ in range(n):
-            eng.multiply_device(0, X.data_ptr(), Y.data_ptr(), B, stream=sp, **c)
-        b.record(stream)
-        torch.cuda.synchronize(dev)
-        return a.elapsed_time(b) / n
+            eng.multiply_device(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, **c)
+        return timed_loop(torch, stream, lambda: eng.multiply_device(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp,
+                                                                     **c), n)
 
     tuning = {}
     if args.variant == 0:
-        default_ms = timed(20, variant=3)
+        tuning["default_vps"] = B * 1000.0 / timed(20, variant=3)
         if not args.no_tune:
             t0 = time.perf_counter()
-            eng.autotune(0, X.data_ptr(), Y.data_ptr(), B, stream=sp, reps=3)
-            tuning = {"autotune_s": round(time.perf_counter() - t0, 2),
-                      "table": [int(v) for v in eng.level_variants(0, B)]}
-        tuning["default_vps"] = B * 1000.0 / default_ms
+            eng.autotune(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, reps=3)
+            tuning["autotune_s"] = round(time.perf_counter() - t0, 2)
+            tuning["autotuned_table"] = [int(v) for v in eng.level_variants(sr, B)]
+            auto_ms = timed(30)
+            tuning["autotuned_vps"] = B * 1000.0 / auto_ms
+            if learn.MODEL_PATH.exists():
+                model = learn.Mlp.load(learn.MODEL_PATH)
+                t0 = time.perf_counter()
+                learn.choose_learned(eng, plan, model, sr, B)
+                tuning["learned_choice_s"] = round(time.perf_counter() - t0, 3)
+                tuning["learned_table"] = [int(v) for v in eng.level_variants(sr, B)]
+                learned_ms = timed(30)
+                tuning["learned_vps"] = B * 1000.0 / learned_ms
+                tuning["learned_regret_vs_autotuner"] = learned_ms / auto_ms - 1.0
+                tuning["headline"] = "learned"
+            else:
+                tuning["headline"] = "autotuned (no trained cost model present)"
 
     for _ in range(args.warmup):
         step()
@@ -296,9 +475,9 @@ def main():
     ms_per_step = ms / args.steps
     value = ws * B * args.steps / (ms / 1000.0)
 
-    # ---- per-launch times (same kernels, launched one by one) for the roofline
+    # ---- per-launch times (the same kernels launched one by one) for the roofline
     reps = 5
-    lt = np.mean([eng.time_launches(0, X.data_ptr(), Y.data_ptr(), B, stream=sp, variant=args.variant or 0)
+    lt = np.mean([eng.time_launches(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, variant=args.variant)
                   for _ in range(reps)], axis=0)
     level_ms = float(lt[1:].sum())       # k_level launches: levels + final fold
     if args.dump_launches:
@@ -308,45 +487,40 @@ def main():
             o = int(ops[i]) if 1 <= i < len(ops) else 0
             em = int(ems[i - 1]) if 1 <= i <= len(ems) else 0
             log(f"{i}\t{t_ms:.4f}\t{o}\t{em}")
-    alg_total = plan.alg_bytes(0, B)
-    alg_pro = 8.0 * (st["ref_alpha"] - 1) + 4.0 * st["n_vals"] + 4.0 * cols * B + 4.0 * rows * B
+    alg_total = plan.alg_bytes(sr, B)
+    alg_pro = 8.0 * (st["ref_alpha"] - 1) + 4.0 * st["n_vals"] + 4.0 * cols * words + 4.0 * rows * words
     alg_level = alg_total - alg_pro      # 12 N_L + 8 E + 8 E_T
     peak, peak_kind = measured_peak_hbm()
     achieved = alg_level / (level_ms / 1000.0) / 1e9
     step_gbs = alg_total / (ms_per_step / 1000.0) / 1e9
-    traffic_file = REPO / "profiles" / "traffic.json"
     traffic = None
-    if traffic_file.exists():
+    tf = REPO / "profiles" / "traffic.json"
+    if tf.exists():
         try:
-            tj = json.loads(traffic_file.read_text())
-            if tj.get("workload") == args.workload and tj.get("B") == B:
-                traffic = tj.get("k_level_bytes_per_multiply")
+            traffic = json.loads(tf.read_text()).get(f"{args.workload}/{args.semiring}/B{B}")
         except Exception:
             traffic = None
 
     # ---- plain per-level sweep, one vector at a time (the reference's scheme)
-    x1 = X[:, :1].contiguous()
-    y1 = torch.empty((rows, 1), dtype=torch.float32, device=dev)
+    x1 = torch.from_numpy(make_inputs(sr, cols, 1, 7).view(np.int32)).to(dev)
+    y1 = torch.empty((rows, 1), dtype=torch.int32, device=dev)
     for _ in range(3):
-        eng.multiply_device(0, x1.data_ptr(), y1.data_ptr(), 1, stream=sp, variant=1)
+        eng.multiply_device(sr, x1.data_ptr(), y1.data_ptr(), 1, stream=sp, variant=1)
     torch.cuda.synchronize(dev)
-    kp = max(10, min(200, args.steps))
-    e0.record(stream)
-    for _ in range(kp):
-        eng.multiply_device(0, x1.data_ptr(), y1.data_ptr(), 1, stream=sp, variant=1)
-    e1.record(stream)
-    torch.cuda.synchronize(dev)
-    plain_vps = kp / (e0.elapsed_time(e1) / 1000.0)
+    kp = max(10, min(100, args.steps))
+    plain_ms = timed_loop(torch, stream,
+                          lambda: eng.multiply_device(sr, x1.data_ptr(), y1.data_ptr(), 1, stream=sp, variant=1), kp)
+    plain_vps = 1000.0 / plain_ms
 
     # ---- end to end through the public API with host buffers (pinned)
-    Xp = torch.from_numpy(Xh).pin_memory()
-    Yp = torch.empty((rows, B), dtype=torch.float32).pin_memory()
+    Xp = torch.from_numpy(Xh.view(np.int32)).pin_memory()
+    Yp = torch.empty((rows, words), dtype=torch.int32).pin_memory()
     for _ in range(3):
-        gmr.lib().gmr_engine_multiply_host(eng._h, 0, Xp.data_ptr(), Yp.data_ptr(), B, None)
+        gmr.lib().gmr_engine_multiply_host(eng._h, sr, Xp.data_ptr(), Yp.data_ptr(), B, None)
     ke = max(10, min(100, args.steps))
     t = time.perf_counter()
     for _ in range(ke):
-        rc = gmr.lib().gmr_engine_multiply_host(eng._h, 0, Xp.data_ptr(), Yp.data_ptr(), B, None)
+        rc = gmr.lib().gmr_engine_multiply_host(eng._h, sr, Xp.data_ptr(), Yp.data_ptr(), B, None)
         if rc:
             raise RuntimeError(gmr.lib().gmr_last_error().decode())
     e2e_s = (time.perf_counter() - t) / ke
@@ -355,35 +529,41 @@ def main():
     out = {
         "metric": METRIC, "value": value, "unit": "vectors/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded mosaic generator + RePair)",
+        "vs_baseline": None, "dtype": dtype_of(sr), "data": "synthetic (seeded generator + RePair)",
         "config": workload_config(args, rows, cols) | {
-            "variant": {0: "auto (autotuned per-launch table, CUDA graph)", 1: "plain", 2: "fused",
-                        3: "graph"}[args.variant], "parallelism": f"replicas x{ws}"},
+            "variant": {0: "auto (learned per-launch table, CUDA graph)", 1: "plain", 2: "fused", 3: "graph",
+                        4: "persistent"}[args.variant], "parallelism": f"replicas x{ws}"},
         "tuning": tuning,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": "k_level (all level launches of one multiply)",
                      "alg_bytes_per_multiply": alg_level, "kernel_ms_per_multiply": level_ms,
                      "step_alg_gbs": step_gbs},
-        "e2e": {"value": e2e_value, "unit": "vectors/s", "h2d_bytes_per_step": int(cols * B * 4),
-                "d2h_bytes_per_step": int(rows * B * 4)},
+        "e2e": {"value": e2e_value, "unit": "vectors/s", "h2d_bytes_per_step": int(cols * words * 4),
+                "d2h_bytes_per_step": int(rows * words * 4)},
         "gpu_launches": int(launches_per_step * args.steps),
         "clocks": clocks,
         "plain_sweep_b1": {"value": plain_vps, "unit": "vectors/s", "speedup": value / ws / plain_vps},
         "grammar": {"ops": st["n_ops"], "depth": st["depth"], "layered_rules": st["ref_layered"],
-                    "passthrough": st["ref_passthrough"], "emit": st["ref_emit"],
-                    "term_emit": st["ref_term_emit"], "terminals": st["ref_alpha"], "plan_s": round(plan_s, 2)}
-        | ginfo,
+                    "passthrough": st["ref_passthrough"], "max_width": st["ref_max_width"],
+                    "emit": st["ref_emit"], "term_emit": st["ref_term_emit"], "terminals": st["ref_alpha"],
+                    "plan_s": round(plan_s, 2)} | ginfo,
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        y0 = Y[:, 0].float().cpu().numpy()
+        yh = Y.cpu().numpy()
+        if sr == 0:
+            y0 = yh.view(np.float32)[:, 0]
+        elif sr == 1:
+            y0 = (yh.view(np.uint32)[:, 0] & np.uint32(1)).astype(np.int64)
+        else:
+            y0 = yh[:, 0]
         threads = os.cpu_count() or 1
-        rate, n, spent, build_s, err = cpu_reference_rate(g, rows, cols, args.cpu_seconds, threads,
-                                                          gpu_y0=y0, x0=Xh[:, 0].copy())
+        rate, n, spent, build_s, check = cpu_reference_rate(g, sr, rows, cols, args.cpu_seconds, threads,
+                                                            gpu_y0=y0, x0=oracle_x(sr, Xh, 0))
         out["cpu_baseline"] = {"value": rate, "unit": "vectors/s", "cores": threads, "kind": "port",
                                "sample": f"{n} single vectors of the same grammar in {spent:.1f} s with the "
                                          f"reference's OpenMP level sweep (restated in oracle/)"}
-        out["rel_err_fp64"] = err
+        out["check"] = check
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:

@@ -102,9 +102,27 @@ __device__ __forceinline__ Vec<T, N> vload(const T* p) {
     return r;
 }
 // Loads of values written earlier in the same multiply (no read-only path).
-template <class T, int N>
+// CG = true loads through L2 only (ld.global.cg): needed inside one launch
+// that reads what other SMs wrote in an earlier phase (the persistent sweep),
+// where a line left in this SM's L1 could be stale.
+template <class T, int N, bool CG = false>
 __device__ __forceinline__ Vec<T, N> vload_rw(const T* p) {
-    return *reinterpret_cast<const Vec<T, N>*>(p);
+    if constexpr (CG) {
+        Vec<T, N> r;
+        if constexpr (N == 4) {
+            uint4 u = __ldcg(reinterpret_cast<const uint4*>(p));
+            memcpy(&r, &u, 16);
+        } else if constexpr (N == 2) {
+            uint2 u = __ldcg(reinterpret_cast<const uint2*>(p));
+            memcpy(&r, &u, 8);
+        } else {
+            uint32_t u = __ldcg(reinterpret_cast<const uint32_t*>(p));
+            memcpy(&r, &u, 4);
+        }
+        return r;
+    } else {
+        return *reinterpret_cast<const Vec<T, N>*>(p);
+    }
 }
 template <class T, int N>
 __device__ __forceinline__ void vstore(T* p, const Vec<T, N>& v) {
@@ -198,7 +216,7 @@ __device__ __forceinline__ int64_t items_of(int64_t units, int G) {
 
 // Per-tile view of the value space: arena slots (refs >= 0) and terminals
 // (refs < 0, T[-ref-1]); the address is selected without branching.
-template <class S, int VEC>
+template <class S, int VEC, bool CG = false>
 struct Values {
     using T = typename S::T;
     const T* arena;
@@ -213,7 +231,9 @@ struct Values {
         const int64_t idx = slot ? (int64_t)c : (-(int64_t)c - 1);
         return (slot ? arena : term) + idx * Bt + lane * VEC;
     }
-    __device__ __forceinline__ Vec<T, VEC> get(int32_t c, int lane) const { return vload_rw<T, VEC>(addr(c, lane)); }
+    __device__ __forceinline__ Vec<T, VEC> get(int32_t c, int lane) const {
+        return vload_rw<T, VEC, CG>(addr(c, lane));
+    }
 };
 
 template <class T>
@@ -223,13 +243,11 @@ __device__ __forceinline__ T* yptr(const SweepArgs& a, int64_t row, int tile, in
 
 // Prologue: Y = zero, T[0] = zero, T[q] = leaf(V[val], X[col]).
 template <class S, int VEC, int GLOG>
-__global__ void __launch_bounds__(256) k_prologue(SweepArgs a) {
+__device__ __forceinline__ void do_prologue(const SweepArgs& a, int tile, int64_t t0, int64_t stride) {
     using T = typename S::T;
-    const int tile = a.t0 + blockIdx.y;
     const int64_t ny = items_of<GLOG>(a.rows, a.G), nt = items_of<GLOG>(a.n_terms, a.G);
     T* Tt = static_cast<T*>(a.T) + (int64_t)tile * a.n_terms * a.Bt;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < ny + nt;
-         t += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t t = t0; t < ny + nt; t += stride) {
         if (t < ny) {
             vstore<T, VEC>(yptr<T>(a, unit_of<GLOG>(t, a.G), tile, lane_of<GLOG>(t, a.G), VEC), vzero<S, VEC>());
         } else {
@@ -252,12 +270,18 @@ __global__ void __launch_bounds__(256) k_prologue(SweepArgs a) {
     }
 }
 
-// Evaluate the ops of one level, two items per thread in flight.
 template <class S, int VEC, int GLOG>
+__global__ void __launch_bounds__(256) k_prologue(SweepArgs a) {
+    do_prologue<S, VEC, GLOG>(a, a.t0 + blockIdx.y, (int64_t)blockIdx.x * blockDim.x + threadIdx.x,
+                              (int64_t)gridDim.x * blockDim.x);
+}
+
+// Evaluate the ops of one level, two items per thread in flight.
+template <class S, int VEC, int GLOG, bool CG = false>
 __device__ __forceinline__ void do_ops(const SweepArgs& a, const LevelArgs& L, int tile, int64_t t0,
                                        int64_t stride) {
     using T = typename S::T;
-    const Values<S, VEC> val(a, tile);
+    const Values<S, VEC, CG> val(a, tile);
     T* out = static_cast<T*>(a.arena) + (int64_t)tile * a.n_ops * a.Bt;
     const int64_t items = items_of<GLOG>(L.n_ops, a.G);
     for (int64_t t = t0; t < items; t += 2 * stride) {
@@ -282,11 +306,11 @@ __device__ __forceinline__ void do_ops(const SweepArgs& a, const LevelArgs& L, i
 }
 
 // One atomic per (emission, word): the reference's emit scheme.
-template <class S, int VEC, int GLOG>
+template <class S, int VEC, int GLOG, bool CG = false>
 __device__ __forceinline__ void do_emits_atomic(const SweepArgs& a, const LevelArgs& L, int tile, int64_t t0,
                                                 int64_t stride) {
     using T = typename S::T;
-    const Values<S, VEC> val(a, tile);
+    const Values<S, VEC, CG> val(a, tile);
     const int64_t items = items_of<GLOG>(L.n_em, a.G);
     for (int64_t t = t0; t < items; t += stride) {
         const int64_t e = L.em_first + unit_of<GLOG>(t, a.G);
@@ -326,11 +350,11 @@ __device__ __forceinline__ Vec<typename S::T, VEC> warp_segment_reduce(Vec<typen
     return tot;
 }
 
-template <class S, int VEC>
+template <class S, int VEC, bool CG = false>
 __device__ __forceinline__ void do_emits_warp(const SweepArgs& a, const LevelArgs& L, int tile, int64_t t0,
                                               int64_t stride) {
     using T = typename S::T;
-    const Values<S, VEC> val(a, tile);
+    const Values<S, VEC, CG> val(a, tile);
     const int lane = threadIdx.x & 31;
     const int64_t n = L.n_em;
     for (int64_t base = t0 - lane; base < n; base += 2 * stride) {  // warp-uniform trip count
@@ -351,11 +375,11 @@ __device__ __forceinline__ void do_emits_warp(const SweepArgs& a, const LevelArg
 
 // Chunked segmented emits: each lane group walks em_chunk consecutive
 // emissions (loads four ahead), accumulating while the row stays the same.
-template <class S, int VEC, int GLOG>
+template <class S, int VEC, int GLOG, bool CG = false>
 __device__ __forceinline__ void do_emits_chunk(const SweepArgs& a, const LevelArgs& L, int tile, int64_t t0,
                                                int64_t stride) {
     using T = typename S::T;
-    const Values<S, VEC> val(a, tile);
+    const Values<S, VEC, CG> val(a, tile);
     const int64_t groups = (L.n_em + L.em_chunk - 1) / L.em_chunk;
     const int64_t items = items_of<GLOG>(groups, a.G);
     const int32_t* rows = L.em_row + L.em_first;
@@ -407,11 +431,11 @@ __device__ __forceinline__ void do_emits_chunk(const SweepArgs& a, const LevelAr
 // updates its row of Y with a plain read-modify-write.  Within a launch every
 // (row, tile) belongs to exactly one segment and levels are separate launches,
 // so no atomics are needed and the (+,x) summation order is fixed.
-template <class S, int VEC, int GLOG>
+template <class S, int VEC, int GLOG, bool CG = false>
 __device__ __forceinline__ void do_emits_rows(const SweepArgs& a, const LevelArgs& L, int tile, int64_t t0,
                                               int64_t stride) {
     using T = typename S::T;
-    const Values<S, VEC> val(a, tile);
+    const Values<S, VEC, CG> val(a, tile);
     const int64_t items = items_of<GLOG>(L.n_seg, a.G);
     for (int64_t t = t0; t < items; t += stride) {
         const int64_t s = L.seg_first + unit_of<GLOG>(t, a.G);
@@ -430,7 +454,7 @@ __device__ __forceinline__ void do_emits_rows(const SweepArgs& a, const LevelArg
         }
         for (; e < e1; ++e) acc0 = voplus<S, VEC>(acc0, val.get(__ldg(L.em_src + e), lane));
         T* yp = yptr<T>(a, row, tile, lane, VEC);
-        vstore<T, VEC>(yp, voplus<S, VEC>(vload_rw<T, VEC>(yp), voplus<S, VEC>(acc0, acc1)));
+        vstore<T, VEC>(yp, voplus<S, VEC>(vload_rw<T, VEC, CG>(yp), voplus<S, VEC>(acc0, acc1)));
     }
 }
 
@@ -449,6 +473,80 @@ __global__ void __launch_bounds__(256) k_level(SweepArgs a, LevelArgs L) {
         const int64_t t0 = (int64_t)(blockIdx.x - L.em_blocks) * blockDim.x + threadIdx.x;
         const int64_t stride = (int64_t)(gridDim.x - L.em_blocks) * blockDim.x;
         do_ops<S, VEC, GLOG>(a, L, tile, t0, stride);
+    }
+}
+
+// Persistent sweep: one cooperative launch walks the prologue and every
+// level, separated by grid barriers.  Each barrier wait is bounded: a block
+// that waits longer than spin_limit polls (or sees another block's failure)
+// records the phase in err[1], sets err[0] and every block returns; the host
+// reads err and reports GMR_ERR_TIMEOUT.  There are no asynchronous copies
+// in flight at a barrier, so returning early leaves nothing pending.
+struct PersistArgs {
+    const int64_t* lvl_off;  // depth + 1 (device)
+    const int64_t* em_off;   // depth + 2
+    const int64_t* seg_off;  // depth + 2
+    int depth;
+    unsigned* bar;           // [0] arrivals, [1] generation
+    int* err;                // [0] failed, [1] phase that gave up
+    unsigned long long spin_limit;
+};
+
+__device__ __forceinline__ bool grid_barrier(const PersistArgs& P, int phase) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* gen = P.bar + 1;
+        volatile int* err = P.err;
+        const unsigned g0 = *gen;  // before arriving: cannot change until every block has arrived
+        __threadfence();
+        const unsigned arrived = atomicAdd(P.bar, 1u) + 1u;
+        if (arrived == gridDim.x) {
+            atomicExch(P.bar, 0u);
+            __threadfence();
+            atomicAdd(P.bar + 1, 1u);
+        } else {
+            unsigned long long n = 0;
+            while (*gen == g0) {
+                if (*err) break;
+                if (++n > P.spin_limit) {
+                    P.err[1] = phase;
+                    __threadfence();
+                    atomicExch(P.err, 1);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile int*)P.err == 0;
+}
+
+template <class S, int VEC, int GLOG, int EMIT>
+__global__ void __launch_bounds__(256) k_persistent(SweepArgs a, LevelArgs L0, PersistArgs P) {
+    const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    do_prologue<S, VEC, GLOG>(a, 0, t0, stride);
+    if (!grid_barrier(P, 0)) return;
+    for (int k = 1; k <= P.depth + 1; ++k) {
+        LevelArgs L = L0;
+        if (k <= P.depth) {
+            L.op_first = P.lvl_off[k - 1];
+            L.n_ops = P.lvl_off[k] - P.lvl_off[k - 1];
+        } else {
+            L.n_ops = 0;
+        }
+        L.em_first = P.em_off[k - 1];
+        L.n_em = P.em_off[k] - P.em_off[k - 1];
+        L.seg_first = P.seg_off[k - 1];
+        L.n_seg = P.seg_off[k] - P.seg_off[k - 1];
+        if constexpr (EMIT == GMR_EMIT_ATOMIC) do_emits_atomic<S, VEC, GLOG, true>(a, L, 0, t0, stride);
+        else if constexpr (EMIT == GMR_EMIT_ROWS) do_emits_rows<S, VEC, GLOG, true>(a, L, 0, t0, stride);
+        else if constexpr (GLOG == 0) do_emits_warp<S, VEC, true>(a, L, 0, t0, stride);
+        else do_emits_chunk<S, VEC, GLOG, true>(a, L, 0, t0, stride);
+        do_ops<S, VEC, GLOG, true>(a, L, 0, t0, stride);
+        if (!grid_barrier(P, k)) return;
     }
 }
 
@@ -500,6 +598,7 @@ static_assert(kNumEmitVariants * 2 == GMR_N_LEVEL_VARIANTS, "variant table size"
 struct Launch {
     int semiring, B, Bw, VEC, G, variant, emit, chunk;
     int Bt, ntile, tile_levels;
+    unsigned long long spin_limit;
     std::vector<uint8_t> lv;  // per-launch variant (index = launch slot), empty = uniform emit/chunk
     bool operator==(const Launch& o) const {
         return semiring == o.semiring && B == o.B && Bw == o.Bw && VEC == o.VEC && variant == o.variant &&
@@ -525,6 +624,9 @@ struct gmr_engine {
     std::vector<int64_t> lvl_off, em_off, seg_off;
     gmr::DevBuf ops, op_c, em_src, em_row, seg_row, seg_start, term_val, term_col, V;
     gmr::DevBuf arena, T, hX, hY;  // scratch
+    gmr::DevBuf d_lvl_off, d_em_off, d_seg_off, sync;  // persistent variant: level tables, barrier + error words
+    int* status_host = nullptr;                           // pinned copy of the last persistent error words
+    bool last_persistent = false;
     cudaStream_t own_stream = nullptr;
     std::vector<gmr::GraphEntry> graphs;
     std::map<std::pair<int, int>, std::vector<uint8_t>> level_variants;  // (semiring, B) -> per-launch variant
@@ -532,7 +634,8 @@ struct gmr_engine {
     int sm_count = 152;
     std::mutex mu;
     std::vector<gmr::DevBuf*> schedule_bufs() {
-        return {&ops, &op_c, &em_src, &em_row, &seg_row, &seg_start, &term_val, &term_col, &V};
+        return {&ops, &op_c, &em_src, &em_row, &seg_row, &seg_start, &term_val, &term_col, &V,
+                &d_lvl_off, &d_em_off, &d_seg_off, &sync};
     }
 };
 
@@ -691,6 +794,94 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
     GMR_CUDA(cudaGetLastError());
 }
 
+template <class S, int VEC, int GLOG, int EMIT>
+static void launch_persistent_emit(gmr_engine* e, const Launch& lc, const SweepArgs& a, const LevelArgs& L0,
+                                   const PersistArgs& P, cudaStream_t st) {
+    auto kernel = k_persistent<S, VEC, GLOG, EMIT>;
+    int per_sm = 0;
+    GMR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0));
+    if (per_sm < 1) throw Error(GMR_ERR_STATE, "persistent kernel cannot be resident");
+    const int grid = per_sm * e->sm_count;
+    SweepArgs aa = a;
+    LevelArgs ll = L0;
+    PersistArgs pp = P;
+    void* args[] = {&aa, &ll, &pp};
+    GMR_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(kernel), dim3(grid), dim3(256), args, 0, st));
+    (void)lc;
+}
+
+template <class S, int VEC, int GLOG>
+static void launch_persistent_t(gmr_engine* e, const Launch& lc, const void* X, void* Y, cudaStream_t st,
+                                int64_t& launches) {
+    if (t_timer) t_timer->mark();
+    SweepArgs a;
+    a.arena = e->arena.p;
+    a.T = e->T.p;
+    a.Y = Y;
+    a.X = X;
+    a.V = static_cast<const float*>(e->V.p);
+    a.term_val = static_cast<const int32_t*>(e->term_val.p);
+    a.term_col = static_cast<const int32_t*>(e->term_col.p);
+    a.n_terms = e->n_terms;
+    a.n_ops = e->n_ops;
+    a.rows = e->rows;
+    a.ldx = lc.Bw;
+    a.ldy = lc.Bw;
+    a.Bt = lc.Bt;
+    a.G = lc.G;
+    a.t0 = 0;
+    LevelArgs L{};
+    L.ops = static_cast<const int2*>(e->ops.p);
+    L.op_c = e->has_coeff ? static_cast<const float*>(e->op_c.p) : nullptr;
+    L.em_src = static_cast<const int32_t*>(e->em_src.p);
+    L.em_row = static_cast<const int32_t*>(e->em_row.p);
+    L.seg_row = static_cast<const int32_t*>(e->seg_row.p);
+    L.seg_start = static_cast<const int64_t*>(e->seg_start.p);
+    L.em_chunk = lc.chunk > 0 ? lc.chunk : 16;
+    PersistArgs P;
+    P.lvl_off = static_cast<const int64_t*>(e->d_lvl_off.p);
+    P.em_off = static_cast<const int64_t*>(e->d_em_off.p);
+    P.seg_off = static_cast<const int64_t*>(e->d_seg_off.p);
+    P.depth = e->depth;
+    P.bar = static_cast<unsigned*>(e->sync.p);
+    P.err = reinterpret_cast<int*>(static_cast<unsigned char*>(e->sync.p) + 8);
+    P.spin_limit = lc.spin_limit;
+    GMR_CUDA(cudaMemsetAsync(e->sync.p, 0, 16, st));
+    if (lc.emit == GMR_EMIT_ATOMIC) launch_persistent_emit<S, VEC, GLOG, GMR_EMIT_ATOMIC>(e, lc, a, L, P, st);
+    else if (lc.emit == GMR_EMIT_ROWS) launch_persistent_emit<S, VEC, GLOG, GMR_EMIT_ROWS>(e, lc, a, L, P, st);
+    else launch_persistent_emit<S, VEC, GLOG, GMR_EMIT_SEGMENTED>(e, lc, a, L, P, st);
+    ++launches;
+    if (t_timer) t_timer->mark();
+    GMR_CUDA(cudaMemcpyAsync(e->status_host, P.err, 8, cudaMemcpyDeviceToHost, st));
+}
+
+template <class S>
+static void launch_persistent_s(gmr_engine* e, const Launch& lc, const void* X, void* Y, cudaStream_t st,
+                                int64_t& n) {
+    if (lc.VEC == 4) {
+        switch (lc.G) {
+            case 1: return launch_persistent_t<S, 4, 0>(e, lc, X, Y, st, n);
+            case 2: return launch_persistent_t<S, 4, 1>(e, lc, X, Y, st, n);
+            case 4: return launch_persistent_t<S, 4, 2>(e, lc, X, Y, st, n);
+            case 8: return launch_persistent_t<S, 4, 3>(e, lc, X, Y, st, n);
+            case 16: return launch_persistent_t<S, 4, 4>(e, lc, X, Y, st, n);
+            case 32: return launch_persistent_t<S, 4, 5>(e, lc, X, Y, st, n);
+            default: return launch_persistent_t<S, 4, -1>(e, lc, X, Y, st, n);
+        }
+    }
+    if (lc.VEC == 2 && lc.G == 1) return launch_persistent_t<S, 2, 0>(e, lc, X, Y, st, n);
+    if (lc.VEC == 1 && lc.G == 1) return launch_persistent_t<S, 1, 0>(e, lc, X, Y, st, n);
+    if (lc.VEC == 2) return launch_persistent_t<S, 2, -1>(e, lc, X, Y, st, n);
+    return launch_persistent_t<S, 1, -1>(e, lc, X, Y, st, n);
+}
+
+static void launch_persistent(gmr_engine* e, const Launch& lc, const void* X, void* Y, cudaStream_t st,
+                              int64_t& n) {
+    if (lc.semiring == GMR_PLUS_TIMES) launch_persistent_s<SPlus>(e, lc, X, Y, st, n);
+    else if (lc.semiring == GMR_BOOLEAN) launch_persistent_s<SBool>(e, lc, X, Y, st, n);
+    else launch_persistent_s<STrop>(e, lc, X, Y, st, n);
+}
+
 template <class S>
 static void launch_chain_s(gmr_engine* e, const Launch& lc, const void* X, void* Y, cudaStream_t st,
                            int64_t& n) {
@@ -733,7 +924,7 @@ static Launch resolve_launch(gmr_engine* e, int semiring, int B, const void* X, 
     lc.Bw = words_per_slot(semiring, B);
     const int asked = cfg ? cfg->variant : GMR_VARIANT_AUTO;
     lc.variant = asked == GMR_VARIANT_AUTO ? GMR_VARIANT_GRAPH : asked;
-    if (lc.variant == GMR_VARIANT_PERSISTENT) lc.variant = GMR_VARIANT_GRAPH;  // not specialised yet
+    lc.spin_limit = cfg && cfg->spin_limit > 0 ? (unsigned long long)cfg->spin_limit : 20000000ull;
     if (asked == GMR_VARIANT_AUTO && !(cfg && cfg->emit_mode)) {
         auto it = e->level_variants.find({semiring, B});
         if (it != e->level_variants.end()) lc.lv = it->second;
@@ -743,6 +934,7 @@ static Launch resolve_launch(gmr_engine* e, int semiring, int B, const void* X, 
     lc.chunk = cfg && cfg->ops_per_cta > 0 ? cfg->ops_per_cta : 16;
     int bt = cfg && cfg->vec_tile > 0 ? cfg->vec_tile : auto_tile(e, lc.Bw);
     if (bt > lc.Bw || lc.Bw % bt != 0) bt = lc.Bw;  // tiles must divide the batch
+    if (lc.variant == GMR_VARIANT_PERSISTENT) bt = lc.Bw;  // one tile: the whole batch in one launch
     lc.Bt = bt;
     lc.ntile = lc.Bw / bt;
     lc.tile_levels = cfg && cfg->tile_levels > 0 ? cfg->tile_levels : e->depth;
@@ -818,6 +1010,9 @@ static void multiply_device(gmr_engine* e, int semiring, const void* X, void* Y,
         }
         GMR_CUDA(cudaGraphLaunch(hit->exec, st));
         launches = hit->launches;
+    } else if (lc.variant == GMR_VARIANT_PERSISTENT) {
+        e->last_persistent = true;
+        launch_persistent(e, lc, X, Y, st, launches);
     } else {
         launch_chain(e, lc, X, Y, st, launches);
     }
@@ -878,6 +1073,13 @@ extern "C" int gmr_engine_create(const gmr_plan* p, int device, gmr_engine** out
             upload(p->seg_row, e->seg_row);
             upload(p->seg_start, e->seg_start);
             upload(p->term_val, e->term_val);
+            upload(p->lvl_off, e->d_lvl_off);
+            upload(p->em_off, e->d_em_off);
+            upload(p->seg_off, e->d_seg_off);
+            e->sync.ensure(16);
+            GMR_CUDA(cudaMemset(e->sync.p, 0, 16));
+            GMR_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&e->status_host), 16, cudaHostAllocDefault));
+            std::memset(e->status_host, 0, 16);
             upload(p->term_col, e->term_col);
             upload(p->V, e->V);
             GMR_CUDA(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking));
@@ -885,6 +1087,7 @@ extern "C" int gmr_engine_create(const gmr_plan* p, int device, gmr_engine** out
         } catch (...) {
             for (auto* b : e->schedule_bufs()) b->release();
             if (e->own_stream) cudaStreamDestroy(e->own_stream);
+            if (e->status_host) cudaFreeHost(e->status_host);
             throw;
         }
         *out = e.release();
@@ -915,9 +1118,13 @@ extern "C" int gmr_engine_multiply_host(gmr_engine* e, int semiring, const void*
         e->hY.ensure(yb);
         cudaStream_t st = e->own_stream;
         if (xb) GMR_CUDA(cudaMemcpyAsync(e->hX.p, hX, xb, cudaMemcpyHostToDevice, st));
+        e->last_persistent = false;
         multiply_device(e, semiring, e->hX.p, e->hY.p, B, cfg, st);
         if (yb) GMR_CUDA(cudaMemcpyAsync(hY, e->hY.p, yb, cudaMemcpyDeviceToHost, st));
         GMR_CUDA(cudaStreamSynchronize(st));
+        if (e->last_persistent && e->status_host[0] != 0)
+            throw Error(GMR_ERR_TIMEOUT, "persistent sweep: a grid-barrier wait gave up at phase " +
+                                             std::to_string(e->status_host[1]) + "; Y is not valid");
     });
 }
 
@@ -1021,6 +1228,14 @@ extern "C" int gmr_engine_autotune(gmr_engine* e, int semiring, const void* dX, 
     });
 }
 
+extern "C" int gmr_engine_status(const gmr_engine* e, int* failed, int* phase) {
+    return guarded([&] {
+        if (!e) throw Error(GMR_ERR_ARG, "null engine");
+        if (failed) *failed = e->status_host ? e->status_host[0] : 0;
+        if (phase) *phase = e->status_host ? e->status_host[1] : 0;
+    });
+}
+
 extern "C" int64_t gmr_engine_last_launches(const gmr_engine* e) { return e ? e->last_launches : -1; }
 
 extern "C" int64_t gmr_engine_device_bytes(const gmr_engine* e) {
@@ -1043,9 +1258,123 @@ extern "C" void gmr_engine_free(gmr_engine* e) {
         for (auto* b : e->schedule_bufs()) b->release();
         for (auto* b : {&e->arena, &e->T, &e->hX, &e->hY}) b->release();
         if (e->own_stream) cudaStreamDestroy(e->own_stream);
+        if (e->status_host) cudaFreeHost(e->status_host);
         if (prev >= 0) cudaSetDevice(prev);
     }
     delete e;
+}
+
+// ------------------------------------------------------------------ packed multi-grammar launch
+// Several engines (grammars of uneven size, each with its own X, Y, B and
+// semiring) multiplied by ONE graph launch: the capture forks one branch per
+// engine (its own stream), so the small grammars' short tails run beside the
+// big grammars' wide levels instead of after them.
+struct gmr_pack {
+    std::vector<gmr_engine*> engines;
+    cudaStream_t origin = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> join;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<gmr::Launch> key_lc;
+    std::vector<const void*> key_x;
+    std::vector<void*> key_y, key_arena;
+    int64_t launches = 0;
+    int device = 0;
+};
+
+extern "C" int gmr_pack_create(gmr_engine* const* engines, int n, gmr_pack** out) {
+    return guarded([&] {
+        if (!engines || n < 1 || !out) throw Error(GMR_ERR_ARG, "bad argument");
+        auto p = std::make_unique<gmr_pack>();
+        for (int i = 0; i < n; ++i) {
+            if (!engines[i]) throw Error(GMR_ERR_ARG, "null engine");
+            if (engines[i]->device != engines[0]->device) throw Error(GMR_ERR_ARG, "engines on different devices");
+            for (int j = 0; j < i; ++j)
+                if (engines[j] == engines[i]) throw Error(GMR_ERR_ARG, "an engine appears twice");
+            p->engines.push_back(engines[i]);
+        }
+        p->device = engines[0]->device;
+        DeviceGuard dg(p->device);
+        GMR_CUDA(cudaStreamCreateWithFlags(&p->origin, cudaStreamNonBlocking));
+        GMR_CUDA(cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming));
+        p->join.resize(n);
+        for (auto& ev : p->join) GMR_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        *out = p.release();
+    });
+}
+
+extern "C" int gmr_pack_multiply(gmr_pack* p, const int* semirings, const void* const* dX, void* const* dY,
+                                 const int* B, void* stream) {
+    return guarded([&] {
+        if (!p || !semirings || !dX || !dY || !B) throw Error(GMR_ERR_ARG, "null argument");
+        const int n = (int)p->engines.size();
+        std::vector<gmr_engine*> order(p->engines);
+        std::sort(order.begin(), order.end());
+        std::vector<std::unique_lock<std::mutex>> locks;
+        for (auto* e : order) locks.emplace_back(e->mu);
+        DeviceGuard dg(p->device);
+        std::vector<Launch> lcs;
+        for (int i = 0; i < n; ++i) {
+            gmr_engine* e = p->engines[i];
+            if (semirings[i] < 0 || semirings[i] > 2) throw Error(GMR_ERR_ARG, "unknown semiring");
+            if (B[i] < 1) throw Error(GMR_ERR_ARG, "B must be >= 1");
+            if (((uintptr_t)dX[i] | (uintptr_t)dY[i]) % 4 != 0) throw Error(GMR_ERR_ARG, "misaligned X or Y");
+            Launch lc = resolve_launch(e, semirings[i], B[i], dX[i], dY[i], nullptr);
+            ensure_scratch(e, lc.Bw);
+            lcs.push_back(lc);
+        }
+        bool hit = p->exec != nullptr && p->key_lc.size() == (size_t)n;
+        for (int i = 0; hit && i < n; ++i)
+            hit = p->key_lc[i] == lcs[i] && p->key_x[i] == dX[i] && p->key_y[i] == dY[i] &&
+                  p->key_arena[i] == p->engines[i]->arena.p;
+        if (!hit) {
+            if (p->exec) cudaGraphExecDestroy(p->exec);
+            p->exec = nullptr;
+            cudaGraph_t graph = nullptr;
+            GMR_CUDA(cudaStreamBeginCapture(p->origin, cudaStreamCaptureModeThreadLocal));
+            int64_t total = 0;
+            try {
+                GMR_CUDA(cudaEventRecord(p->fork, p->origin));
+                for (int i = 0; i < n; ++i) {
+                    gmr_engine* e = p->engines[i];
+                    GMR_CUDA(cudaStreamWaitEvent(e->own_stream, p->fork, 0));
+                    launch_chain(e, lcs[i], dX[i], dY[i], e->own_stream, total);
+                    GMR_CUDA(cudaEventRecord(p->join[i], e->own_stream));
+                    GMR_CUDA(cudaStreamWaitEvent(p->origin, p->join[i], 0));
+                }
+            } catch (...) {
+                cudaStreamEndCapture(p->origin, &graph);
+                if (graph) cudaGraphDestroy(graph);
+                throw;
+            }
+            GMR_CUDA(cudaStreamEndCapture(p->origin, &graph));
+            cudaError_t ie = cudaGraphInstantiate(&p->exec, graph, 0);
+            cudaGraphDestroy(graph);
+            GMR_CUDA(ie);
+            p->key_lc = lcs;
+            p->key_x.assign(dX, dX + n);
+            p->key_y.assign(dY, dY + n);
+            p->key_arena.clear();
+            for (auto* e : p->engines) p->key_arena.push_back(e->arena.p);
+            p->launches = total;
+        }
+        GMR_CUDA(cudaGraphLaunch(p->exec, static_cast<cudaStream_t>(stream)));
+    });
+}
+
+extern "C" int64_t gmr_pack_last_launches(const gmr_pack* p) { return p ? p->launches : -1; }
+
+extern "C" void gmr_pack_free(gmr_pack* p) {
+    if (!p) return;
+    int prev = -1;
+    cudaGetDevice(&prev);
+    cudaSetDevice(p->device);
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    for (auto ev : p->join) cudaEventDestroy(ev);
+    if (p->fork) cudaEventDestroy(p->fork);
+    if (p->origin) cudaStreamDestroy(p->origin);
+    if (prev >= 0) cudaSetDevice(prev);
+    delete p;
 }
 
 // ------------------------------------------------------------------ no-allocation entry point

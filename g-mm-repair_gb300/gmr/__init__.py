@@ -401,8 +401,14 @@ class Engine:
         self.close()
 
     @staticmethod
-    def _cfg(variant=0, emit_mode=0, ops_per_cta=0, vec_tile=0, tile_levels=0):
-        return Config(variant, vec_tile, ops_per_cta, emit_mode, tile_levels)
+    def _cfg(variant=0, emit_mode=0, ops_per_cta=0, vec_tile=0, tile_levels=0, spin_limit=0):
+        return Config(variant, vec_tile, ops_per_cta, emit_mode, tile_levels, spin_limit)
+
+    def status(self):
+        """(failed, phase) of the last persistent multiply (after a stream synchronize)."""
+        f, p = C.c_int(), C.c_int()
+        _check(lib().gmr_engine_status(self._h, C.byref(f), C.byref(p)))
+        return f.value, p.value
 
     def multiply_device(self, semiring, x_ptr: int, y_ptr: int, B: int, stream: int = 0, **cfg):
         c = self._cfg(**cfg)
@@ -469,6 +475,37 @@ class Engine:
     @property
     def device_bytes(self) -> int:
         return int(lib().gmr_engine_device_bytes(self._h))
+
+
+class Pack:
+    """Several engines multiplied by one CUDA-graph launch (one branch per engine)."""
+
+    def __init__(self, engines):
+        self.engines = list(engines)
+        arr = (C.c_void_p * len(self.engines))(*[e._h.value for e in self.engines])
+        h = C.c_void_p()
+        _check(lib().gmr_pack_create(arr, len(self.engines), C.byref(h)))
+        self._h = h
+
+    def multiply_device(self, semirings, x_ptrs, y_ptrs, Bs, stream: int = 0):
+        n = len(self.engines)
+        sr = (C.c_int * n)(*[semiring_id(s) for s in semirings])
+        xs = (C.c_void_p * n)(*x_ptrs)
+        ys = (C.c_void_p * n)(*y_ptrs)
+        bs = (C.c_int * n)(*Bs)
+        _check(lib().gmr_pack_multiply(self._h, sr, xs, ys, bs, C.c_void_p(stream)))
+
+    @property
+    def last_launches(self) -> int:
+        return int(lib().gmr_pack_last_launches(self._h))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().gmr_pack_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        self.close()
 
 
 # ---------------------------------------------------------------- legacy ABI

@@ -63,7 +63,7 @@ class DevicePlan(C.Structure):
 
 class Config(C.Structure):
     _fields_ = [("variant", C.c_int), ("vec_tile", C.c_int), ("ops_per_cta", C.c_int), ("emit_mode", C.c_int),
-                ("tile_levels", C.c_int)]
+                ("tile_levels", C.c_int), ("spin_limit", C.c_int)]
 
 
 P = C.c_void_p
@@ -114,7 +114,12 @@ _SIGS = {
     "gmr_engine_get_level_variants": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(C.c_uint8), C.c_int,
                                                 C.POINTER(C.c_int)]),
     "gmr_engine_autotune": (C.c_int, [P, C.c_int, P, P, C.c_int, P, C.c_int, F32P, C.c_int]),
+    "gmr_engine_status": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "gmr_engine_last_launches": (C.c_int64, [P]),
+    "gmr_pack_create": (C.c_int, [C.POINTER(P), C.c_int, C.POINTER(P)]),
+    "gmr_pack_multiply": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(P), C.POINTER(P), C.POINTER(C.c_int), P]),
+    "gmr_pack_last_launches": (C.c_int64, [P]),
+    "gmr_pack_free": (None, [P]),
     "gmr_engine_device_bytes": (C.c_int64, [P]),
     "gmr_engine_free": (None, [P]),
     "gmr_plan_launch_features": (C.c_int, [P, C.c_int, C.c_int, F32P, C.c_int, C.POINTER(C.c_int)]),

@@ -222,6 +222,8 @@ typedef struct {
     int emit_mode;    /* GMR_EMIT_* */
     int tile_levels;  /* levels 1..tile_levels run tile by tile, the rest
                          all tiles per launch (0 = by level size) */
+    int spin_limit;   /* GMR_VARIANT_PERSISTENT: polls a grid-barrier wait
+                         may take before it gives up (0 = 20,000,000) */
 } gmr_config;
 enum {
     GMR_VARIANT_AUTO = 0,
@@ -311,6 +313,25 @@ void gmr_mlp_free(gmr_mlp* m);
  * to pred[slot * GMR_N_LEVEL_VARIANTS + v] when pred != NULL. */
 int gmr_engine_choose_learned(gmr_engine* e, const gmr_plan* p, const gmr_mlp* m, int semiring, int B,
                               float* pred, int cap);
+
+/* Status of the engine's last GMR_VARIANT_PERSISTENT multiply, valid once the
+ * stream it ran on has been synchronized: *failed != 0 when a grid-barrier
+ * wait gave up (Y of that multiply is not valid), *phase = where (0 =
+ * prologue, k = level k).  gmr_engine_multiply_host checks it itself and
+ * returns GMR_ERR_TIMEOUT. */
+int gmr_engine_status(const gmr_engine* e, int* failed, int* phase);
+/* Several engines in one launch: grammars of uneven size, each with its own
+ * semiring, X, Y and B, multiplied by one CUDA-graph launch that runs one
+ * branch per engine concurrently (each branch = that engine's AUTO chain).
+ * The graph is captured on the first call with a given set of arguments and
+ * replayed afterwards.  All engines must live on the same device; an engine
+ * may belong to one pack call at a time. */
+typedef struct gmr_pack gmr_pack;
+int gmr_pack_create(gmr_engine* const* engines, int n, gmr_pack** out);
+int gmr_pack_multiply(gmr_pack* p, const int* semirings, const void* const* dX, void* const* dY,
+                      const int* B, void* stream);
+int64_t gmr_pack_last_launches(const gmr_pack* p);
+void gmr_pack_free(gmr_pack* p);
 
 /* Kernel launches issued by the calling thread's last multiply. */
 int64_t gmr_engine_last_launches(const gmr_engine* e);

@@ -99,6 +99,8 @@ CONFIGS = [
     dict(variant=gmr.VARIANT_FUSED, emit_mode=gmr.EMIT_ATOMIC, vec_tile=2),
     dict(variant=gmr.VARIANT_GRAPH, emit_mode=gmr.EMIT_ROWS, vec_tile=4, tile_levels=2),
     dict(variant=gmr.VARIANT_GRAPH, emit_mode=gmr.EMIT_SEGMENTED, vec_tile=8, ops_per_cta=5),
+    dict(variant=gmr.VARIANT_PERSISTENT),                                  # one cooperative launch
+    dict(variant=gmr.VARIANT_PERSISTENT, emit_mode=gmr.EMIT_ROWS),
 ]
 
 
@@ -179,6 +181,56 @@ def test_autotuned_and_mixed_tables(case, sr):
         check(sr, Y, ref)
     eng.set_level_variants(sr, B, None)
     assert eng.level_variants(sr, B) is None
+
+
+def test_persistent_barrier_timeout_reports_status(c1):
+    """A grid-barrier wait limited to one poll gives up: the host gets
+    GMR_ERR_TIMEOUT, and the next multiply on the same context is correct."""
+    eng = c1["eng"]
+    rng = np.random.default_rng(3)
+    x = rng.uniform(-1, 1, (5000, 8)).astype(np.float32)
+    timeouts = 0
+    for _ in range(3):
+        try:
+            eng.multiply(x, 0, B=8, variant=gmr.VARIANT_PERSISTENT, spin_limit=1)
+        except gmr.GmrError as e:
+            assert e.code == 7 and "gave up" in str(e)
+            timeouts += 1
+    assert timeouts >= 1
+    failed, phase = eng.status()
+    assert failed in (0, 1)
+    y = eng.multiply(x, 0, B=8, variant=gmr.VARIANT_PERSISTENT)
+    assert eng.status()[0] == 0
+    ref = c1["sched"].sweep_f64(0, c1["V"], x[:, 3], 20000, 5000)
+    assert relmax(y[:, 3], ref) <= TOL
+
+
+def test_packed_multi_grammar_launch():
+    """Eight uneven grammars, each with its own semiring and B, in one graph launch."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(10)
+    engines, scheds, args = [], [], []
+    for i in range(8):
+        rows, cols = int(rng.integers(300, 3000)), int(rng.integers(64, 700))
+        m = gmr.gen_mosaic(rows, cols, 16, 0.02, 0.002, 10 + i, threads=4)
+        g = gmr.repair(m, 4)
+        engines.append(gmr.Engine(gmr.Plan.build(g, rows, cols)))
+        scheds.append((O.RefSchedule(g.alpha, g.rules(), g.C()), g.values(), rows, cols))
+        sr, B = i % 3, [1, 4, 16, 64][i % 4]
+        X = random_X(sr, cols, B, 50 + i)
+        Xw = engine_inputs(sr, X)
+        dX = torch.from_numpy(Xw.view(np.int32)).cuda()
+        dY = torch.zeros((rows, Xw.shape[1]), dtype=torch.int32, device="cuda")
+        args.append((sr, B, X, dX, dY))
+    pack = gmr.Pack(engines)
+    for _ in range(2):  # capture, then replay
+        pack.multiply_device([a[0] for a in args], [a[3].data_ptr() for a in args], [a[4].data_ptr() for a in args],
+                             [a[1] for a in args], stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert pack.last_launches >= 8 * 3
+    for (sched, V, rows, cols), (sr, B, X, dX, dY) in zip(scheds, args):
+        Yw = dY.cpu().numpy().view({0: np.float32, 1: np.uint32, 2: np.int32}[sr])
+        check(sr, engine_outputs(sr, Yw, B), oracle_columns(sched, sr, V, X, rows, cols))
 
 
 def test_unittest_grammar_runlength():
