@@ -287,6 +287,50 @@ def run_reference(args):
     return 0
 
 
+def cusparse_baseline(torch, args, rows, cols, B, n=20):
+    """cuSPARSE CSR SpMM (through torch.sparse) on the UNCOMPRESSED matrix of the
+    same workload, fp32, same B: the reference's library baseline
+    (gpu-engine/cusparse_test.cu:432-502).  Reported beside the engine; not the
+    path under test."""
+    import gmr
+
+    if args.workload not in MOSAICS or args.semiring != "plustimes":
+        return None
+    r, c, F, sw, mu, seed = MOSAICS[args.workload]
+    t0 = time.perf_counter()
+    m = gmr.gen_mosaic(r, c, F, sw, mu, seed)
+    codes = m.codes()
+    del m
+    ends = np.flatnonzero(codes == 0)
+    crow = np.zeros(rows + 1, dtype=np.int64)
+    crow[1:len(ends) + 1] = ends - np.arange(len(ends))
+    crow[len(ends) + 1:] = crow[len(ends)]
+    colv = (codes[codes != 0] - 1).astype(np.int32)  # value index 0: every stored value is 1
+    del codes
+    nnz = int(colv.size)
+    try:
+        A = torch.sparse_csr_tensor(torch.from_numpy(crow).cuda(), torch.from_numpy(colv).to(torch.int64).cuda(),
+                                    torch.ones(nnz, device="cuda"), size=(rows, cols))
+    except RuntimeError as e:  # out of memory or unsupported
+        return {"unavailable": str(e).splitlines()[0]}
+    build_s = time.perf_counter() - t0
+    X = torch.rand((cols, B), device="cuda") * 2 - 1
+    stream = torch.cuda.current_stream()
+    for _ in range(3):
+        Yc = A @ X
+    ms = timed_loop(torch, stream, lambda: A @ X, n)
+    x1 = X[:, :1].contiguous()
+    for _ in range(3):
+        A @ x1
+    ms1 = timed_loop(torch, stream, lambda: A @ x1, n)
+    out = {"spmm_vps": B * 1000.0 / ms, "spmm_ms": ms, "spmv_vps": 1000.0 / ms1, "nnz": nnz,
+           "csr_bytes": int(nnz * 8 + (rows + 1) * 8), "build_s": round(build_s, 1),
+           "how": "torch.sparse_csr_tensor @ dense (cuSPARSE), fp32, int64 indices"}
+    del A, Yc
+    torch.cuda.empty_cache()
+    return out
+
+
 def timed_loop(torch, stream, fn, n):
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     a.record(stream)
@@ -372,6 +416,7 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=6.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--dump-launches", action="store_true", help="per-launch times and level sizes to stderr")
+    ap.add_argument("--no-cusparse", action="store_true", help="skip the cuSPARSE CSR baseline")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.semiring is None:
@@ -549,6 +594,12 @@ def main():
                     "emit": st["ref_emit"], "term_emit": st["ref_term_emit"], "terminals": st["ref_alpha"],
                     "plan_s": round(plan_s, 2)} | ginfo,
     }
+    if rank == 0 and ws == 1 and not args.no_cusparse:
+        del eng  # free the engine's device memory before building the CSR baseline
+        torch.cuda.synchronize(dev)
+        out["cusparse_csr"] = cusparse_baseline(torch, args, rows, cols, B)
+        if out["cusparse_csr"] and "spmm_vps" in out["cusparse_csr"]:
+            out["cusparse_csr"]["engine_speedup"] = value / out["cusparse_csr"]["spmm_vps"]
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         yh = Y.cpu().numpy()
         if sr == 0:

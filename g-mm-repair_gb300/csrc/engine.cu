@@ -593,7 +593,10 @@ static constexpr EmitVariant kEmitVariants[] = {
     {GMR_EMIT_ATOMIC, 0}};
 static constexpr int kNumEmitVariants = 5;
 static constexpr int kOpsCtasPerSm[] = {32, 4};
-static_assert(kNumEmitVariants * 2 == GMR_N_LEVEL_VARIANTS, "variant table size");
+// v = emit + 5 * grid + 10 * chunked (chunked: fold the emissions of a level
+// one source chunk at a time, see gmr_engine::ch_*)
+static_assert(kNumEmitVariants * 2 * 2 == GMR_N_LEVEL_VARIANTS, "variant table size");
+static constexpr int64_t kChunkSlots = 1 << 19;  // source slots per chunk (64 MB of values at 32 words)
 
 struct Launch {
     int semiring, B, Bw, VEC, G, variant, emit, chunk;
@@ -625,6 +628,14 @@ struct gmr_engine {
     gmr::DevBuf ops, op_c, em_src, em_row, seg_row, seg_start, term_val, term_col, V;
     gmr::DevBuf arena, T, hX, hY;  // scratch
     gmr::DevBuf d_lvl_off, d_em_off, d_seg_off, sync;  // persistent variant: level tables, barrier + error words
+    // The emissions again, ordered by (source chunk, row, source) within each
+    // level, with row segments per chunk: chunk c of level k covers source
+    // slots [c, c+1) * kChunkSlots of that level (terminals for level 0).
+    // Level k's chunks are [ch_off[k], ch_off[k+1]); chunk i's emissions
+    // [ch_em[i], ch_em[i+1]) and segments [ch_seg[i], ch_seg[i+1]).
+    gmr::DevBuf em_src_c, em_row_c, seg_row_c, seg_start_c;
+    std::vector<int64_t> ch_off, ch_em, ch_seg;
+    bool chunked = false;
     int* status_host = nullptr;                           // pinned copy of the last persistent error words
     bool last_persistent = false;
     cudaStream_t own_stream = nullptr;
@@ -635,7 +646,7 @@ struct gmr_engine {
     std::mutex mu;
     std::vector<gmr::DevBuf*> schedule_bufs() {
         return {&ops, &op_c, &em_src, &em_row, &seg_row, &seg_start, &term_val, &term_col, &V,
-                &d_lvl_off, &d_em_off, &d_seg_off, &sync};
+                &d_lvl_off, &d_em_off, &d_seg_off, &sync, &em_src_c, &em_row_c, &seg_row_c, &seg_start_c};
     }
 };
 
@@ -699,9 +710,9 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
         int64_t cap = std::max<int64_t>(1, (int64_t)e->sm_count * 32 / nt);  // grid-stride beyond this
         return (int)std::max<int64_t>(1, std::min(b, cap));
     };
-    auto after = [&] {
+    auto after = [&](bool mark = true) {
         ++launches;
-        if (t_timer) t_timer->mark();
+        if (t_timer && mark) t_timer->mark();
     };
     {
         int64_t items = (e->rows + e->n_terms) * (int64_t)lc.G;
@@ -722,11 +733,13 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
         L.seg_start = static_cast<const int64_t*>(e->seg_start.p);
         const int slot = k_ops >= 1 ? k_ops : e->depth + 1;  // launch slot of this level launch
         int emit = lc.emit, chunk = lc.chunk, ops_cap = kOpsCtasPerSm[0];
+        bool by_chunk = false;
         if (!lc.lv.empty() && slot < (int)lc.lv.size()) {
             const int v = lc.lv[slot] % GMR_N_LEVEL_VARIANTS;
             emit = kEmitVariants[v % kNumEmitVariants].emit;
             chunk = kEmitVariants[v % kNumEmitVariants].chunk;
-            ops_cap = kOpsCtasPerSm[v / kNumEmitVariants];
+            ops_cap = kOpsCtasPerSm[(v / kNumEmitVariants) % 2];
+            by_chunk = v >= 2 * kNumEmitVariants;
         }
         if (lc.variant == GMR_VARIANT_PLAIN) emit = GMR_EMIT_ATOMIC;
         if (chunk <= 0) chunk = 16;
@@ -742,22 +755,22 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
             L.seg_first = e->seg_off[k_em];
             nseg = e->seg_off[k_em + 1] - e->seg_off[k_em];
         }
-        auto em_items = [&]() -> int64_t {
-            if (emit == GMR_EMIT_ATOMIC) return nem * lc.G;
-            if (emit == GMR_EMIT_ROWS) return nseg * lc.G;
-            if (GLOG == 0) return (nem + 1) / 2;  // two warp-blocks per warp iteration
-            return (nem + chunk - 1) / chunk * lc.G;
+        auto em_items = [&](int64_t ne, int64_t ns) -> int64_t {
+            if (emit == GMR_EMIT_ATOMIC) return ne * lc.G;
+            if (emit == GMR_EMIT_ROWS) return ns * lc.G;
+            if (GLOG == 0) return (ne + 1) / 2;  // two warp-blocks per warp iteration
+            return (ne + chunk - 1) / chunk * lc.G;
         };
-        auto go = [&](int64_t no, bool with_em) {
-            LevelArgs M = L;
+        auto go = [&](const LevelArgs& base, int64_t no, int64_t ne, int64_t ns, bool mark) {
+            LevelArgs M = base;
             M.n_ops = no;
-            M.n_em = with_em ? nem : 0;
-            M.n_seg = with_em ? nseg : 0;
-            if (no == 0 && M.n_em == 0) {
-                if (t_timer && !split) t_timer->mark();  // keep one timing slot per level launch
+            M.n_em = ne;
+            M.n_seg = ns;
+            if (no == 0 && ne == 0) {
+                if (t_timer && mark && !split) t_timer->mark();  // keep one timing slot per level launch
                 return;
             }
-            int eb = M.n_em > 0 ? blocks_for(em_items(), nt) : 0;
+            int eb = ne > 0 ? blocks_for(em_items(ne, ns), nt) : 0;
             int ob = no > 0 ? std::min<int>(blocks_for((no * lc.G + 1) / 2, nt),
                                             std::max(1, e->sm_count * ops_cap / nt)) : 0;
             M.em_blocks = eb;
@@ -768,13 +781,29 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
                 k_level<S, VEC, GLOG, GMR_EMIT_ROWS><<<grid, TPB, 0, st>>>(s, M);
             else
                 k_level<S, VEC, GLOG, GMR_EMIT_SEGMENTED><<<grid, TPB, 0, st>>>(s, M);
-            after();
+            after(mark);
         };
         if (split) {  // plain: emissions and ops in separate launches
-            go(0, true);
-            go(nops, false);
-        } else {
-            go(nops, true);
+            go(L, 0, nem, nseg, true);
+            go(L, nops, 0, 0, true);
+            return;
+        }
+        const int64_t nch = (by_chunk && e->chunked && k_em >= 0) ? e->ch_off[k_em + 1] - e->ch_off[k_em] : 0;
+        if (nch < 2) {
+            go(L, nops, nem, nseg, true);
+            return;
+        }
+        // one launch per source chunk of level k_em; the first also evaluates level k_ops
+        LevelArgs C = L;
+        C.em_src = static_cast<const int32_t*>(e->em_src_c.p);
+        C.em_row = static_cast<const int32_t*>(e->em_row_c.p);
+        C.seg_row = static_cast<const int32_t*>(e->seg_row_c.p);
+        C.seg_start = static_cast<const int64_t*>(e->seg_start_c.p);
+        for (int64_t c = 0; c < nch; ++c) {
+            const int64_t i = e->ch_off[k_em] + c;
+            C.em_first = e->ch_em[i];
+            C.seg_first = e->ch_seg[i];
+            go(C, c == 0 ? nops : 0, e->ch_em[i + 1] - e->ch_em[i], e->ch_seg[i + 1] - e->ch_seg[i], c == nch - 1);
         }
     };
     const int D = e->depth;
@@ -1044,6 +1073,68 @@ struct Nvml {
 
 using namespace gmr;
 
+// The chunked emission order (see gmr_engine::ch_*), built when some level
+// has more than one source chunk: a stable counting sort of each level's
+// (row, source)-ordered emissions by source chunk, then row segments per chunk.
+// The chunk size is kChunkSlots unless the environment variable
+// GMR_CHUNK_SLOTS (read when the engine is created) sets another one.
+static void build_chunked_emissions(const gmr_plan& p, gmr_engine& e) {
+    const int D = p.depth;
+    int64_t kChunkSlots = gmr::kChunkSlots;
+    if (const char* env = std::getenv("GMR_CHUNK_SLOTS")) {
+        long long v = std::atoll(env);
+        if (v >= 1) kChunkSlots = v;
+    }
+    bool any = false;
+    for (int k = 0; k <= D && !any; ++k) {
+        const int64_t width = k == 0 ? p.n_terms() : p.lvl_off[k] - p.lvl_off[k - 1];
+        any = width > kChunkSlots && p.em_off[k + 1] > p.em_off[k];
+    }
+    if (!any) return;
+    const int64_t E = (int64_t)p.em_src.size();
+    std::vector<int32_t> src(E), row(E), srow;
+    std::vector<int64_t> sstart;
+    e.ch_off.assign(D + 2, 0);
+    e.ch_em.clear();
+    e.ch_seg.clear();
+    for (int k = 0; k <= D; ++k) {
+        e.ch_off[k] = (int64_t)e.ch_em.size();
+        const int64_t lo = p.em_off[k], hi = p.em_off[k + 1];
+        if (hi == lo) continue;
+        const int64_t base = k == 0 ? 0 : p.lvl_off[k - 1];
+        auto chunk_of = [&](int32_t c) { return (c >= 0 ? (int64_t)c - base : -(int64_t)c - 1) / kChunkSlots; };
+        int64_t nc = 0;
+        for (int64_t j = lo; j < hi; ++j) nc = std::max(nc, chunk_of(p.em_src[j]) + 1);
+        std::vector<int64_t> pos(nc + 1, 0);
+        for (int64_t j = lo; j < hi; ++j) pos[chunk_of(p.em_src[j]) + 1]++;
+        for (int64_t c = 0; c < nc; ++c) pos[c + 1] += pos[c];
+        std::vector<int64_t> start(pos.begin(), pos.end());
+        for (int64_t j = lo; j < hi; ++j) {
+            const int64_t d = lo + pos[chunk_of(p.em_src[j])]++;
+            src[d] = p.em_src[j];
+            row[d] = p.em_row[j];
+        }
+        for (int64_t c = 0; c < nc; ++c) {
+            e.ch_em.push_back(lo + start[c]);
+            e.ch_seg.push_back((int64_t)srow.size());
+            for (int64_t j = lo + start[c]; j < lo + start[c + 1]; ++j)
+                if (j == lo + start[c] || row[j] != row[j - 1]) {
+                    srow.push_back(row[j]);
+                    sstart.push_back(j);
+                }
+        }
+    }
+    e.ch_off[D + 1] = (int64_t)e.ch_em.size();
+    e.ch_em.push_back(E);
+    e.ch_seg.push_back((int64_t)srow.size());
+    sstart.push_back(E);
+    upload(src, e.em_src_c);
+    upload(row, e.em_row_c);
+    upload(srow, e.seg_row_c);
+    upload(sstart, e.seg_start_c);
+    e.chunked = true;
+}
+
 extern "C" int gmr_engine_create(const gmr_plan* p, int device, gmr_engine** out) {
     return guarded([&] {
         if (!p || !out) throw Error(GMR_ERR_ARG, "null argument");
@@ -1078,6 +1169,7 @@ extern "C" int gmr_engine_create(const gmr_plan* p, int device, gmr_engine** out
             upload(p->seg_off, e->d_seg_off);
             e->sync.ensure(16);
             GMR_CUDA(cudaMemset(e->sync.p, 0, 16));
+            build_chunked_emissions(*p, *e);
             GMR_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&e->status_host), 16, cudaHostAllocDefault));
             std::memset(e->status_host, 0, 16);
             upload(p->term_col, e->term_col);

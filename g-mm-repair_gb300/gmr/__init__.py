@@ -442,7 +442,7 @@ class Engine:
                                               C.byref(n)))
         return ms[: n.value].copy()
 
-    N_LEVEL_VARIANTS = 10
+    N_LEVEL_VARIANTS = 20
 
     def set_level_variants(self, semiring, B: int, table):
         """Install a per-launch variant table (len depth + 2) used by AUTO multiplies; None clears."""

@@ -28,7 +28,7 @@ from . import _lib as L
 from . import Engine, Grammar, Plan, _check, gen_copy_graph, gen_mosaic, lib, repair, semiring_id
 
 N_BASE = 16
-N_VAR = 10
+N_VAR = 20
 IN_DIM = N_BASE + N_VAR
 MODEL_PATH = Path(__file__).resolve().parent / "models" / "cost_model.gmrmlp"
 

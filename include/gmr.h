@@ -257,13 +257,15 @@ int gmr_engine_time_launches(gmr_engine* e, int semiring, const void* dX, void* 
 /* Per-launch kernel variants (the autotuner's and the learned model's
  * decision table).  Launch slot 0 is the prologue (ignored), slot k the launch
  * of level k (rules of level k + emissions of level k-1), slot depth+1 the
- * final fold.  Variant v = e + 5 * g: e = 0 segmented chunk 16, 1 chunk 8,
- * 2 chunk 32 (for one lane per emission all three are the warp-shuffle
- * reduction), 3 row-owned, 4 one atomic per emission; g = 0 up to 32 CTAs
- * per SM evaluate the rules, g = 1 up to 4 (more rules per CTA).  An
- * installed table is used by GMR_VARIANT_AUTO multiplies of that
- * (semiring, B).  n = depth + 2; v = NULL clears. */
-#define GMR_N_LEVEL_VARIANTS 10
+ * final fold.  Variant v = e + 5 * g + 10 * c: e = 0 segmented chunk 16,
+ * 1 chunk 8, 2 chunk 32 (for one lane per emission all three are the
+ * warp-shuffle reduction), 3 row-owned, 4 one atomic per emission; g = 0 up
+ * to 32 CTAs per SM evaluate the rules, g = 1 up to 4 (more rules per CTA);
+ * c = 1 folds the emissions one source chunk (2^19 slots of the level) at a
+ * time, one launch per chunk, so the chunk's values stay in L2.  An installed
+ * table is used by GMR_VARIANT_AUTO multiplies of that (semiring, B).
+ * n = depth + 2; v = NULL clears. */
+#define GMR_N_LEVEL_VARIANTS 20
 int gmr_engine_set_level_variants(gmr_engine* e, int semiring, int B, const uint8_t* v, int n);
 int gmr_engine_get_level_variants(const gmr_engine* e, int semiring, int B, uint8_t* v, int cap, int* n);
 /* Exhaustive autotuner: times every variant on every launch (median of

@@ -233,6 +233,23 @@ def test_packed_multi_grammar_launch():
         check(sr, engine_outputs(sr, Yw, B), oracle_columns(sched, sr, V, X, rows, cols))
 
 
+@pytest.mark.parametrize("sr", range(3))
+def test_chunked_emission_passes(case, sr, monkeypatch):
+    """Folding emissions one source chunk at a time (tiny chunks here, so every
+    level has several) gives the same results in every emission mode."""
+    monkeypatch.setenv("GMR_CHUNK_SLOTS", "7")
+    eng = gmr.Engine(case["plan"])
+    monkeypatch.delenv("GMR_CHUNK_SLOTS")
+    rows, cols = int(case["rows"]), int(case["cols"])
+    for B in (1, 32):
+        X = random_X(sr, cols, B, 300 + B)
+        ref = oracle_columns(case["sched"], sr, case["V"], X, rows, cols)
+        for v in (10, 12, 13, 14, 17):  # chunked: segmented 16 / 32, row-owned, atomic; 4 CTAs per SM
+            eng.set_level_variants(sr, B, np.full(eng.depth + 2, v, dtype=np.uint8))
+            Y = engine_outputs(sr, eng.multiply(engine_inputs(sr, X), sr, B=B), B)
+            check(sr, Y, ref)
+
+
 def test_unittest_grammar_runlength():
     """cpu_selftest.cpp:374-467 grammar (run-length rule, coefficient 3)."""
     g = gmr.Grammar.from_arrays(5, [[1, 2], [3, 5], [6, 0], [7, 5]], [8, 0], [1.5, 2.5], kinds=[0, 0, 1, 0],

@@ -37,7 +37,7 @@ def test_model_inputs_one_hot():
 
 def test_model_file_round_trip_and_checksum(tmp_path):
     m = Lr.Mlp.create(seed=3)
-    assert m.n_params == 26 * 64 + 64 + 2 * (64 * 64 + 64) + 64 + 1
+    assert m.n_params == Lr.IN_DIM * 64 + 64 + 2 * (64 * 64 + 64) + 64 + 1
     m.set_norm(np.linspace(0, 1, Lr.IN_DIM), np.linspace(1, 2, Lr.IN_DIM))
     m.save(tmp_path / "m.gmrmlp")
     m2 = Lr.Mlp.load(tmp_path / "m.gmrmlp")
