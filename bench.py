@@ -258,77 +258,44 @@ def workload_config(args, rows, cols):
 
 
 def run_reference(args):
+    """The reference's CPU implementation of the path on the host cores: one
+    step = one vector through the OpenMP layered sweep (gpu_engine_test.cu:49-104,
+    restated in oracle/); the schedule is built once, outside the timed steps."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
     if args.workload == "pack8":
         print(json.dumps({"impl": "reference", "unavailable": "pack8 has no single-grammar CPU path"}))
         return 0
+    from oracle import oracle as O
+
     g, rows, cols, _ = workload_grammar(args)
     threads = os.cpu_count() or 1
     sr = SR_IDS[args.semiring]
-    per_step = []
-    for _ in range(args.warmup + args.steps):
-        rate, n, spent, build_s, _ = cpu_reference_rate(g, sr, rows, cols, args.ref_seconds, threads)
-        per_step.append(rate)
-    v = statistics.median(per_step[args.warmup:])
+    sched = O.RefSchedule(g.alpha, g.rules(), g.C())
+    V = g.values().astype(np.float32)
+    Xh = make_inputs(sr, cols, max(args.steps + args.warmup, 1) if sr != 1 else 32, 1)
+    times = []
+    for i in range(args.warmup + args.steps):
+        x = oracle_x(sr, Xh, i % Xh.shape[1] if sr != 1 else i % 32)
+        t = time.perf_counter()
+        sched.cpu_reference(sr, V, x, rows, cols, threads=threads)
+        times.append(time.perf_counter() - t)
+    timed = times[args.warmup:]
+    v = len(timed) / sum(timed)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "vectors/s", "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": dtype_of(sr), "data": "synthetic",
-        "config": workload_config(args, rows, cols),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sum(timed) / len(timed),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype_of(sr),
+        "data": "synthetic", "config": workload_config(args, rows, cols),
         "cpu_baseline": {"value": v, "unit": "vectors/s", "cores": threads, "kind": "port",
-                         "sample": f"each step: the reference's OpenMP layered CPU sweep (restated in oracle/) on "
-                                   f"1-20 single vectors of the same grammar for ~{args.ref_seconds:.0f} s; "
-                                   f"no batched CPU path exists, so vectors/s = 1/t"},
+                         "sample": f"{len(timed)} single vectors of the same grammar, one per step, through the "
+                                   f"reference's OpenMP layered CPU sweep (restated in oracle/), {threads} threads; "
+                                   f"no batched CPU path exists, so vectors/s = steps / time"},
         "e2e": {"value": v, "unit": "vectors/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
-
-
-def cusparse_baseline(torch, args, rows, cols, B, n=20):
-    """cuSPARSE CSR SpMM (through torch.sparse) on the UNCOMPRESSED matrix of the
-    same workload, fp32, same B: the reference's library baseline
-    (gpu-engine/cusparse_test.cu:432-502).  Reported beside the engine; not the
-    path under test."""
-    import gmr
-
-    if args.workload not in MOSAICS or args.semiring != "plustimes":
-        return None
-    r, c, F, sw, mu, seed = MOSAICS[args.workload]
-    t0 = time.perf_counter()
-    m = gmr.gen_mosaic(r, c, F, sw, mu, seed)
-    codes = m.codes()
-    del m
-    ends = np.flatnonzero(codes == 0)
-    crow = np.zeros(rows + 1, dtype=np.int64)
-    crow[1:len(ends) + 1] = ends - np.arange(len(ends))
-    crow[len(ends) + 1:] = crow[len(ends)]
-    colv = (codes[codes != 0] - 1).astype(np.int32)  # value index 0: every stored value is 1
-    del codes
-    nnz = int(colv.size)
-    try:
-        A = torch.sparse_csr_tensor(torch.from_numpy(crow).cuda(), torch.from_numpy(colv).to(torch.int64).cuda(),
-                                    torch.ones(nnz, device="cuda"), size=(rows, cols))
-    except RuntimeError as e:  # out of memory or unsupported
-        return {"unavailable": str(e).splitlines()[0]}
-    build_s = time.perf_counter() - t0
-    X = torch.rand((cols, B), device="cuda") * 2 - 1
-    stream = torch.cuda.current_stream()
-    for _ in range(3):
-        Yc = A @ X
-    ms = timed_loop(torch, stream, lambda: A @ X, n)
-    x1 = X[:, :1].contiguous()
-    for _ in range(3):
-        A @ x1
-    ms1 = timed_loop(torch, stream, lambda: A @ x1, n)
-    out = {"spmm_vps": B * 1000.0 / ms, "spmm_ms": ms, "spmv_vps": 1000.0 / ms1, "nnz": nnz,
-           "csr_bytes": int(nnz * 8 + (rows + 1) * 8), "build_s": round(build_s, 1),
-           "how": "torch.sparse_csr_tensor @ dense (cuSPARSE), fp32, int64 indices"}
-    del A, Yc
-    torch.cuda.empty_cache()
-    return out
 
 
 def timed_loop(torch, stream, fn, n):
@@ -413,7 +380,6 @@ def main():
                          "4 persistent")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner and the learned choice")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--ref-seconds", type=float, default=6.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--dump-launches", action="store_true", help="per-launch times and level sizes to stderr")
     ap.add_argument("--no-cusparse", action="store_true", help="skip the cuSPARSE CSR baseline")

@@ -687,6 +687,7 @@ static thread_local LaunchTimer* t_timer = nullptr;
 template <class S, int VEC, int GLOG>
 static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void* Y, cudaStream_t st,
                            int64_t& launches) {
+    if (lc.ntile > 65535) throw Error(GMR_ERR_RANGE, "batch too wide: more than 65535 right-hand-side tiles");
     if (t_timer) t_timer->mark();
     SweepArgs a;
     a.arena = e->arena.p;

@@ -250,6 +250,26 @@ def test_chunked_emission_passes(case, sr, monkeypatch):
             check(sr, Y, ref)
 
 
+def test_allocation_failure_is_reported():
+    """A batch whose scratch cannot be allocated returns GMR_ERR_OOM (nothing is
+    launched) and the engine keeps working for a normal batch afterwards."""
+    torch = pytest.importorskip("torch")
+    c = load_case("mosaic_300x64")
+    g = gmr.Grammar.from_arrays(int(c["alpha"]), c["rules"], c["C"], c["V"])
+    plan = gmr.Plan.build(g, 300, 64)
+    eng = gmr.Engine(plan)
+    s = plan.stats
+    huge_B = 1 << 27
+    assert (s["n_ops"] + s["n_terms"]) * huge_B * 4 > 400e9  # beyond the device's memory
+    x = torch.zeros(16, dtype=torch.float32, device="cuda")
+    with pytest.raises(gmr.GmrError) as e:
+        eng.multiply_device(0, x.data_ptr(), x.data_ptr(), huge_B)
+    assert e.value.code == 5 and "cudaMalloc" in str(e.value)
+    sched = O.RefSchedule(int(c["alpha"]), c["rules"], c["C"])
+    X = random_X(0, 64, 4, 1)
+    check(0, eng.multiply(X, 0, B=4), oracle_columns(sched, 0, c["V"], X, 300, 64))
+
+
 def test_unittest_grammar_runlength():
     """cpu_selftest.cpp:374-467 grammar (run-length rule, coefficient 3)."""
     g = gmr.Grammar.from_arrays(5, [[1, 2], [3, 5], [6, 0], [7, 5]], [8, 0], [1.5, 2.5], kinds=[0, 0, 1, 0],
