@@ -366,6 +366,54 @@ def run_pack8(args):
     return 0
 
 
+def run_other_op(args):
+    """Left product (Y = X^T M) or fixpoint iteration timed on the workload's grammar."""
+    import torch
+
+    import gmr
+
+    g, rows, cols, ginfo = workload_grammar(args)
+    plan = gmr.Plan.build(g, rows, cols)
+    eng = gmr.Engine(plan)
+    sr, B = SR_IDS[args.semiring], args.B
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    out = {"metric": f"{args.op} vectors/s", "unit": "vectors/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "higher_is_better": True, "dtype": dtype_of(sr), "data": "synthetic",
+           "config": workload_config(args, rows, cols) | {"op": args.op}}
+    if args.op == "left":
+        t0 = time.perf_counter()
+        eng.enable_left(plan)
+        out["prepare_s"] = round(time.perf_counter() - t0, 2)
+        X = torch.from_numpy(make_inputs(sr, rows, B, 5).view(np.int32)).cuda()
+        Y = torch.empty((cols, X.shape[1]), dtype=torch.int32, device="cuda")
+        for _ in range(args.warmup):
+            eng.multiply_left_device(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp)
+        ms = timed_loop(torch, stream, lambda: eng.multiply_left_device(sr, X.data_ptr(), Y.data_ptr(), B,
+                                                                         stream=sp), args.steps)
+        out |= {"value": B * 1000.0 / ms, "ms_per_step": ms}
+    else:
+        if rows != cols:
+            print(json.dumps({"unavailable": "fixpoint needs a square matrix (graph workload)"}))
+            return 0
+        X0 = make_inputs(sr, cols, B, 5)
+        if sr == 2:
+            X0 = np.where(X0 == INT_MAX, np.int32(1_000_000_000), X0).astype(np.int32)
+        X = torch.from_numpy(X0.view(np.int32)).cuda()
+        Y = torch.empty_like(X)
+        eng.multiply_device(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp)  # graph capture
+        Xs = X.clone()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        iters = eng.fixpoint_device(sr, X.data_ptr(), Y.data_ptr(), B, max_iters=10_000, stream=sp)
+        torch.cuda.synchronize()
+        s = time.perf_counter() - t
+        out |= {"value": B / s, "ms_per_step": s * 1000.0, "iterations": iters,
+                "ms_per_iteration": s * 1000.0 / max(iters, 1), "start_nonzero_words": int((Xs != 0).sum())}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -383,6 +431,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--dump-launches", action="store_true", help="per-launch times and level sizes to stderr")
     ap.add_argument("--no-cusparse", action="store_true", help="skip the cuSPARSE CSR baseline")
+    ap.add_argument("--op", choices=["right", "left", "fixpoint"], default="right",
+                    help="right: Y = M X (the headline); left: Y = X^T M; fixpoint: X <- X (+) M X to convergence")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.semiring is None:
@@ -391,6 +441,8 @@ def main():
         return run_reference(args)
     if args.workload == "pack8":
         return run_pack8(args)
+    if args.op != "right":
+        return run_other_op(args)
 
     import torch
 

@@ -636,6 +636,9 @@ struct gmr_engine {
     gmr::DevBuf em_src_c, em_row_c, seg_row_c, seg_start_c;
     std::vector<int64_t> ch_off, ch_em, ch_seg;
     bool chunked = false;
+    // Left product (y = x^T M): reverse adjacency uploaded by gmr_engine_enable_left.
+    gmr::DevBuf par_off, par_src, erow_off, erow_row, tcol_off, tcol_q;
+    bool left_ready = false;
     int* status_host = nullptr;                           // pinned copy of the last persistent error words
     bool last_persistent = false;
     cudaStream_t own_stream = nullptr;
@@ -646,7 +649,8 @@ struct gmr_engine {
     std::mutex mu;
     std::vector<gmr::DevBuf*> schedule_bufs() {
         return {&ops, &op_c, &em_src, &em_row, &seg_row, &seg_start, &term_val, &term_col, &V,
-                &d_lvl_off, &d_em_off, &d_seg_off, &sync, &em_src_c, &em_row_c, &seg_row_c, &seg_start_c};
+                &d_lvl_off, &d_em_off, &d_seg_off, &sync, &em_src_c, &em_row_c, &seg_row_c, &seg_start_c,
+                &par_off, &par_src, &erow_off, &erow_row, &tcol_off, &tcol_q};
     }
 };
 
@@ -1355,6 +1359,237 @@ extern "C" void gmr_engine_free(gmr_engine* e) {
         if (prev >= 0) cudaSetDevice(prev);
     }
     delete e;
+}
+
+// ------------------------------------------------------------------ left product
+// y = x^T M (y[c] = (+)_r x[r] (x) M[r][c]) over the same grammar, top-down:
+// the "down" value of a symbol is the (+) of its parents' down values (times
+// the run-length coefficient for a left child) and of x over the rows that
+// emit it; levels run from the top down (a parent is always above its
+// children), then every column folds leaf(V, down) over its terminals.
+namespace gmr {
+
+struct LeftArgs {
+    void* down;  // [n_ops][Bw] (the arena)
+    const void* X;  // [rows][Bw]
+    void* Y;        // [cols][Bw]
+    const int64_t* par_off;
+    const int32_t* par_src;
+    const int64_t* erow_off;
+    const int32_t* erow_row;
+    const int64_t* tcol_off;
+    const int32_t* tcol_q;
+    const float* op_c;
+    const float* V;
+    const int32_t* term_val;
+    int64_t n_ops, first, count;
+    int Bw, G;
+};
+
+template <class S, int VEC, int GLOG>
+__device__ __forceinline__ Vec<typename S::T, VEC> left_down(const LeftArgs& a, int64_t u, int lane) {
+    using T = typename S::T;
+    Vec<T, VEC> acc = vzero<S, VEC>();
+    const T* down = static_cast<const T*>(a.down);
+    for (int64_t e = __ldg(a.par_off + u), e1 = __ldg(a.par_off + u + 1); e < e1; ++e) {
+        const int32_t p = __ldg(a.par_src + e);
+        const int64_t pp = p >= 0 ? p : ~p;
+        Vec<T, VEC> v = vload_rw<T, VEC>(down + pp * a.Bw + lane * VEC);
+        if (a.op_c && p >= 0) {
+            const float c = __ldg(a.op_c + pp);
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) v.v[j] = S::apply(v.v[j], c);
+        }
+        acc = voplus<S, VEC>(acc, v);
+    }
+    const T* X = static_cast<const T*>(a.X);
+    for (int64_t e = __ldg(a.erow_off + u), e1 = __ldg(a.erow_off + u + 1); e < e1; ++e)
+        acc = voplus<S, VEC>(acc, vload<T, VEC>(X + (int64_t)__ldg(a.erow_row + e) * a.Bw + lane * VEC));
+    return acc;
+}
+
+template <class S, int VEC, int GLOG>
+__global__ void __launch_bounds__(256) k_left_level(LeftArgs a) {
+    using T = typename S::T;
+    const int64_t items = items_of<GLOG>(a.count, a.G);
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < items; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t u = a.first + unit_of<GLOG>(t, a.G);
+        const int lane = lane_of<GLOG>(t, a.G);
+        vstore<T, VEC>(static_cast<T*>(a.down) + u * a.Bw + lane * VEC, left_down<S, VEC, GLOG>(a, u, lane));
+    }
+}
+
+template <class S, int VEC, int GLOG>
+__global__ void __launch_bounds__(256) k_left_columns(LeftArgs a) {
+    using T = typename S::T;
+    const int64_t items = items_of<GLOG>(a.count, a.G);  // count = cols
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < items; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = unit_of<GLOG>(t, a.G);
+        const int lane = lane_of<GLOG>(t, a.G);
+        Vec<T, VEC> acc = vzero<S, VEC>();
+        for (int64_t i = __ldg(a.tcol_off + c), i1 = __ldg(a.tcol_off + c + 1); i < i1; ++i) {
+            const int32_t q = __ldg(a.tcol_q + i);
+            const Vec<T, VEC> d = left_down<S, VEC, GLOG>(a, a.n_ops + q, lane);
+            const float v = __ldg(a.V + __ldg(a.term_val + q - 1));
+            Vec<T, VEC> l;
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) l.v[j] = S::leaf(v, d.v[j]);
+            acc = voplus<S, VEC>(acc, l);
+        }
+        vstore<T, VEC>(static_cast<T*>(a.Y) + c * a.Bw + lane * VEC, acc);
+    }
+}
+
+template <class S, int VEC, int GLOG>
+static void left_chain_t(gmr_engine* e, int Bw, int G, const void* X, void* Y, cudaStream_t st) {
+    LeftArgs a{};
+    a.down = e->arena.p;
+    a.X = X;
+    a.Y = Y;
+    a.par_off = static_cast<const int64_t*>(e->par_off.p);
+    a.par_src = static_cast<const int32_t*>(e->par_src.p);
+    a.erow_off = static_cast<const int64_t*>(e->erow_off.p);
+    a.erow_row = static_cast<const int32_t*>(e->erow_row.p);
+    a.tcol_off = static_cast<const int64_t*>(e->tcol_off.p);
+    a.tcol_q = static_cast<const int32_t*>(e->tcol_q.p);
+    a.op_c = e->has_coeff ? static_cast<const float*>(e->op_c.p) : nullptr;
+    a.V = static_cast<const float*>(e->V.p);
+    a.term_val = static_cast<const int32_t*>(e->term_val.p);
+    a.n_ops = e->n_ops;
+    a.Bw = Bw;
+    a.G = G;
+    auto blocks = [&](int64_t items) {
+        return (int)std::max<int64_t>(1, std::min<int64_t>((items + 255) / 256, (int64_t)e->sm_count * 32));
+    };
+    for (int k = e->depth; k >= 1; --k) {
+        a.first = e->lvl_off[k - 1];
+        a.count = e->lvl_off[k] - e->lvl_off[k - 1];
+        if (a.count == 0) continue;
+        k_left_level<S, VEC, GLOG><<<blocks(a.count * G), 256, 0, st>>>(a);
+    }
+    a.first = 0;
+    a.count = e->cols;
+    k_left_columns<S, VEC, GLOG><<<blocks((int64_t)e->cols * G), 256, 0, st>>>(a);
+    GMR_CUDA(cudaGetLastError());
+}
+
+template <class S>
+static void left_chain_s(gmr_engine* e, int Bw, const void* X, void* Y, cudaStream_t st) {
+    const bool a16 = ((uintptr_t)X % 16 == 0) && ((uintptr_t)Y % 16 == 0);
+    if (Bw % 4 == 0 && a16) {
+        switch (Bw / 4) {
+            case 1: return left_chain_t<S, 4, 0>(e, Bw, 1, X, Y, st);
+            case 2: return left_chain_t<S, 4, 1>(e, Bw, 2, X, Y, st);
+            case 4: return left_chain_t<S, 4, 2>(e, Bw, 4, X, Y, st);
+            case 8: return left_chain_t<S, 4, 3>(e, Bw, 8, X, Y, st);
+            case 16: return left_chain_t<S, 4, 4>(e, Bw, 16, X, Y, st);
+            case 32: return left_chain_t<S, 4, 5>(e, Bw, 32, X, Y, st);
+            default: return left_chain_t<S, 4, -1>(e, Bw, Bw / 4, X, Y, st);
+        }
+    }
+    if (Bw == 1) return left_chain_t<S, 1, 0>(e, Bw, 1, X, Y, st);
+    return left_chain_t<S, 1, -1>(e, Bw, Bw, X, Y, st);
+}
+
+}  // namespace gmr
+
+extern "C" int gmr_engine_enable_left(gmr_engine* e, gmr_plan* p) {
+    return guarded([&] {
+        if (!e || !p) throw Error(GMR_ERR_ARG, "null argument");
+        if (p->n_ops() != e->n_ops || p->rows != e->rows || p->cols != e->cols)
+            throw Error(GMR_ERR_ARG, "plan does not match the engine");
+        int rc = gmr_plan_prepare_left(p);
+        if (rc != GMR_OK) throw Error(rc, gmr_last_error());
+        std::lock_guard<std::mutex> lk(e->mu);
+        DeviceGuard dg(e->device);
+        upload(p->par_off, e->par_off);
+        upload(p->par_src, e->par_src);
+        upload(p->erow_off, e->erow_off);
+        upload(p->erow_row, e->erow_row);
+        upload(p->tcol_off, e->tcol_off);
+        upload(p->tcol_q, e->tcol_q);
+        e->left_ready = true;
+    });
+}
+
+extern "C" int gmr_engine_multiply_left(gmr_engine* e, int semiring, const void* dX, void* dY, int B,
+                                        void* stream) {
+    return guarded([&] {
+        if (!e) throw Error(GMR_ERR_ARG, "null engine");
+        if (!e->left_ready) throw Error(GMR_ERR_STATE, "call gmr_engine_enable_left first");
+        if (semiring < 0 || semiring > 2) throw Error(GMR_ERR_ARG, "unknown semiring");
+        if (B < 1) throw Error(GMR_ERR_ARG, "B must be >= 1");
+        if ((!dX && e->rows > 0) || (!dY && e->cols > 0)) throw Error(GMR_ERR_ARG, "null X or Y");
+        if (((uintptr_t)dX | (uintptr_t)dY) % 4 != 0) throw Error(GMR_ERR_ARG, "X and Y must be 4-byte aligned");
+        std::lock_guard<std::mutex> lk(e->mu);
+        DeviceGuard dg(e->device);
+        const int Bw = words_per_slot(semiring, B);
+        ensure_scratch(e, Bw);
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        if (semiring == GMR_PLUS_TIMES) left_chain_s<SPlus>(e, Bw, dX, dY, st);
+        else if (semiring == GMR_BOOLEAN) left_chain_s<SBool>(e, Bw, dX, dY, st);
+        else left_chain_s<STrop>(e, Bw, dX, dY, st);
+        e->last_launches = e->depth + 1;
+    });
+}
+
+// ------------------------------------------------------------------ fixpoint iteration
+// x <- x (+) (M (x) x) until nothing changes, for a square matrix in the
+// idempotent semirings: the natural caller of the Boolean and tropical sweeps
+// (reachability / BFS frontiers, Bellman-Ford relaxation).
+namespace gmr {
+
+template <class S>
+__global__ void k_merge_changed(typename S::T* __restrict__ X, const typename S::T* __restrict__ Y, int64_t n,
+                                int* __restrict__ changed) {
+    bool any = false;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const typename S::T x = X[i], v = S::oplus(x, Y[i]);
+        if (v != x) {
+            X[i] = v;
+            any = true;
+        }
+    }
+    if (__any_sync(0xffffffffu, any) && (threadIdx.x & 31) == 0) atomicExch(changed, 1);
+}
+
+}  // namespace gmr
+
+extern "C" int gmr_engine_fixpoint(gmr_engine* e, int semiring, void* dX, void* dY, int B, int max_iters,
+                                   void* stream, int* iters) {
+    return guarded([&] {
+        if (!e || !dX || !dY) throw Error(GMR_ERR_ARG, "null argument");
+        if (semiring != GMR_BOOLEAN && semiring != GMR_TROPICAL)
+            throw Error(GMR_ERR_ARG, "fixpoint needs an idempotent semiring (boolean or tropical)");
+        if (e->rows != e->cols) throw Error(GMR_ERR_ARG, "fixpoint needs a square matrix");
+        if (B < 1 || max_iters < 0) throw Error(GMR_ERR_ARG, "bad B or max_iters");
+        std::lock_guard<std::mutex> lk(e->mu);
+        DeviceGuard dg(e->device);
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        const int64_t n = (int64_t)e->rows * words_per_slot(semiring, B);
+        e->sync.ensure(16);
+        int* flag = reinterpret_cast<int*>(static_cast<unsigned char*>(e->sync.p) + 8);
+        int it = 0;
+        for (; it < max_iters; ++it) {
+            multiply_device(e, semiring, dX, dY, B, nullptr, st);
+            GMR_CUDA(cudaMemsetAsync(flag, 0, 4, st));
+            const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)e->sm_count * 8));
+            if (semiring == GMR_BOOLEAN)
+                k_merge_changed<SBool><<<blocks, 256, 0, st>>>(static_cast<uint32_t*>(dX),
+                                                              static_cast<const uint32_t*>(dY), n, flag);
+            else
+                k_merge_changed<STrop><<<blocks, 256, 0, st>>>(static_cast<int32_t*>(dX),
+                                                              static_cast<const int32_t*>(dY), n, flag);
+            GMR_CUDA(cudaGetLastError());
+            GMR_CUDA(cudaMemcpyAsync(e->status_host + 2, flag, 4, cudaMemcpyDeviceToHost, st));
+            GMR_CUDA(cudaStreamSynchronize(st));
+            if (e->status_host[2] == 0) {
+                ++it;
+                break;
+            }
+        }
+        if (iters) *iters = it;
+    });
 }
 
 // ------------------------------------------------------------------ packed multi-grammar launch

@@ -88,6 +88,13 @@ struct gmr_plan {
     gmr_plan_stats stats{};
     // B-independent per-slot statistics for the cost-model features (lazy)
     mutable std::vector<double> slot_stats;
+    // Transpose (left product) structures, built by gmr_plan_prepare_left.
+    // Node u = arena slot (u < n_ops) or terminal n_ops + q.  Parents of u:
+    // par_src[par_off[u] .. par_off[u+1]), p >= 0 when u is p's left child,
+    // ~p when it is the right child.  Rows emitting u: erow_row[erow_off[u]..).
+    // Terminals of column c: tcol_q[tcol_off[c] .. tcol_off[c+1]) (q >= 1).
+    std::vector<int64_t> par_off, erow_off, tcol_off;
+    std::vector<int32_t> par_src, erow_row, tcol_q;
 
     int64_t n_ops() const { return (int64_t)op_l.size(); }
     int64_t n_terms() const { return (int64_t)term_val.size() + 1; }

@@ -543,6 +543,42 @@ extern "C" int gmr_plan_launch_features(const gmr_plan* p, int semiring, int B, 
     });
 }
 
+
+extern "C" int gmr_plan_prepare_left(gmr_plan* p) {
+    return guarded([&] {
+        if (!p) throw Error(GMR_ERR_ARG, "null plan");
+        if (!p->par_off.empty()) return;
+        const int64_t n = p->n_ops(), U = p->n_terms(), N = n + U;
+        auto node = [&](int32_t ref) -> int64_t { return ref >= 0 ? (int64_t)ref : n + (-(int64_t)ref - 1); };
+        std::vector<int64_t> po(N + 1, 0), eo(N + 1, 0), co((size_t)p->cols + 1, 0);
+        for (int64_t i = 0; i < n; ++i) {
+            po[node(p->op_l[i]) + 1]++;
+            po[node(p->op_r[i]) + 1]++;
+        }
+        for (size_t e = 0; e < p->em_src.size(); ++e) eo[node(p->em_src[e]) + 1]++;
+        for (size_t q = 0; q < p->term_col.size(); ++q) co[p->term_col[q] + 1]++;
+        for (int64_t u = 0; u < N; ++u) {
+            po[u + 1] += po[u];
+            eo[u + 1] += eo[u];
+        }
+        for (int c = 0; c < p->cols; ++c) co[c + 1] += co[c];
+        std::vector<int32_t> ps((size_t)po[N]), er((size_t)eo[N]), tq(p->term_col.size());
+        std::vector<int64_t> fp(po.begin(), po.end() - 1), fe(eo.begin(), eo.end() - 1), fc(co.begin(), co.end() - 1);
+        for (int64_t i = 0; i < n; ++i) {  // parents in increasing slot order
+            ps[fp[node(p->op_l[i])]++] = (int32_t)i;
+            ps[fp[node(p->op_r[i])]++] = ~(int32_t)i;
+        }
+        for (size_t e = 0; e < p->em_src.size(); ++e) er[fe[node(p->em_src[e])]++] = p->em_row[e];
+        for (size_t q = 0; q < p->term_col.size(); ++q) tq[fc[p->term_col[q]]++] = (int32_t)(q + 1);
+        p->par_off.swap(po);
+        p->erow_off.swap(eo);
+        p->tcol_off.swap(co);
+        p->par_src.swap(ps);
+        p->erow_row.swap(er);
+        p->tcol_q.swap(tq);
+    });
+}
+
 extern "C" int gmr_plan_get_stats(const gmr_plan* p, gmr_plan_stats* s) {
     return guarded([&] {
         if (!p || !s) throw Error(GMR_ERR_ARG, "null argument");
@@ -619,6 +655,12 @@ extern "C" int gmr_plan_array(const gmr_plan* p, int which, const void** ptr, in
             case 10: *ptr = p->seg_off.data(); *n = (int64_t)p->seg_off.size(); break;
             case 11: *ptr = p->seg_row.data(); *n = (int64_t)p->seg_row.size(); break;
             case 12: *ptr = p->seg_start.data(); *n = (int64_t)p->seg_start.size(); break;
+            case 13: *ptr = p->par_off.data(); *n = (int64_t)p->par_off.size(); break;
+            case 14: *ptr = p->par_src.data(); *n = (int64_t)p->par_src.size(); break;
+            case 15: *ptr = p->erow_off.data(); *n = (int64_t)p->erow_off.size(); break;
+            case 16: *ptr = p->erow_row.data(); *n = (int64_t)p->erow_row.size(); break;
+            case 17: *ptr = p->tcol_off.data(); *n = (int64_t)p->tcol_off.size(); break;
+            case 18: *ptr = p->tcol_q.data(); *n = (int64_t)p->tcol_q.size(); break;
             default: throw Error(GMR_ERR_ARG, "unknown plan array");
         }
     });

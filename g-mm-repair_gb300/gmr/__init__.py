@@ -311,7 +311,9 @@ class Plan:
     _ARRAYS = {"op_l": (0, np.int32), "op_r": (1, np.int32), "op_c": (2, np.float32), "lvl_off": (3, np.int64),
                "em_off": (4, np.int64), "em_src": (5, np.int32), "em_row": (6, np.int32),
                "term_val": (7, np.int32), "term_col": (8, np.int32), "V": (9, np.float32),
-               "seg_off": (10, np.int64), "seg_row": (11, np.int32), "seg_start": (12, np.int64)}
+               "seg_off": (10, np.int64), "seg_row": (11, np.int32), "seg_start": (12, np.int64),
+               "par_off": (13, np.int64), "par_src": (14, np.int32), "erow_off": (15, np.int64),
+               "erow_row": (16, np.int32), "tcol_off": (17, np.int64), "tcol_q": (18, np.int32)}
 
     def array(self, name: str) -> np.ndarray:
         which, dt = self._ARRAYS[name]
@@ -321,6 +323,10 @@ class Plan:
 
     def alg_bytes(self, semiring, B: int) -> float:
         return float(lib().gmr_plan_alg_bytes(self._h, semiring_id(semiring), B))
+
+    def prepare_left(self):
+        """Builds the reverse adjacency for the left product (y = x^T M)."""
+        _check(lib().gmr_plan_prepare_left(self._h))
 
     def describe(self) -> str:
         cap = 1 << 16
@@ -443,6 +449,23 @@ class Engine:
         return ms[: n.value].copy()
 
     N_LEVEL_VARIANTS = 20
+
+    def enable_left(self, plan: "Plan"):
+        """Upload the reverse adjacency needed by the left product y = x^T M."""
+        _check(lib().gmr_engine_enable_left(self._h, plan._h))
+
+    def multiply_left_device(self, semiring, x_ptr: int, y_ptr: int, B: int, stream: int = 0):
+        """y[cols][words] = x^T M for x[rows][words] (device pointers)."""
+        _check(lib().gmr_engine_multiply_left(self._h, semiring_id(semiring), C.c_void_p(x_ptr),
+                                              C.c_void_p(y_ptr), B, C.c_void_p(stream)))
+
+    def fixpoint_device(self, semiring, x_ptr: int, y_ptr: int, B: int, max_iters: int = 1000,
+                        stream: int = 0) -> int:
+        """x <- x (+) M x until it stops changing (boolean / tropical, square M); returns the iterations."""
+        it = C.c_int()
+        _check(lib().gmr_engine_fixpoint(self._h, semiring_id(semiring), C.c_void_p(x_ptr), C.c_void_p(y_ptr), B,
+                                         max_iters, C.c_void_p(stream), C.byref(it)))
+        return it.value
 
     def set_level_variants(self, semiring, B: int, table):
         """Install a per-launch variant table (len depth + 2) used by AUTO multiplies; None clears."""

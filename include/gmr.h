@@ -201,7 +201,10 @@ double gmr_plan_alg_bytes(const gmr_plan* p, int semiring, int B);
  * (int64, depth+1), 4 em_off (int64, depth+2), 5 em_src (int32),
  * 6 em_row (int32), 7 term_val (int32), 8 term_col (int32), 9 V (float),
  * 10 seg_off (int64, depth+2), 11 seg_row (int32), 12 seg_start (int64,
- * n_seg+1): the emissions of one (level, row) pair form one row segment.
+ * n_seg+1): the emissions of one (level, row) pair form one row segment;
+ * after gmr_plan_prepare_left: 13 par_off (int64), 14 par_src (int32),
+ * 15 erow_off (int64), 16 erow_row (int32), 17 tcol_off (int64),
+ * 18 tcol_q (int32) (see gmr_plan_prepare_left).
  * *ptr stays valid until gmr_plan_free. */
 int gmr_plan_array(const gmr_plan* p, int which, const void** ptr, int64_t* n);
 /* Human-readable per-level report (the host_scheduler inspector). */
@@ -322,6 +325,32 @@ int gmr_engine_choose_learned(gmr_engine* e, const gmr_plan* p, const gmr_mlp* m
  * prologue, k = level k).  gmr_engine_multiply_host checks it itself and
  * returns GMR_ERR_TIMEOUT. */
 int gmr_engine_status(const gmr_engine* e, int* failed, int* phase);
+/* Left product y = x^T M (y[c] = (+)_r x[r] (x) M[r][c]) over the same
+ * grammar: a top-down sweep (each symbol's value is the (+) of its parents'
+ * values and of x over the rows that emit it), then every column folds
+ * leaf(V, value) over its terminals.  x is [rows][words], y [cols][words]
+ * (words = B, or ceil(B/32) for GMR_BOOLEAN).  gmr_plan_prepare_left builds
+ * the reverse adjacency (parents per symbol, emitting rows per symbol,
+ * terminals per column) on the host; gmr_engine_enable_left uploads it.
+ * The reference has no counterpart in its engine; mm-repair's CPU mat-vec
+ * reports both Ax and xA. */
+int gmr_plan_prepare_left(gmr_plan* p);
+int gmr_engine_enable_left(gmr_engine* e, gmr_plan* p);
+int gmr_engine_multiply_left(gmr_engine* e, int semiring, const void* dX, void* dY, int B, void* stream);
+
+/* Fixpoint iteration x <- x (+) (M (x) x) on a square matrix (rows == cols)
+ * in an idempotent semiring: GMR_BOOLEAN grows every bit-packed frontier to
+ * the set of nodes that reach it (x | Mx, repeated); GMR_TROPICAL relaxes
+ * distances to the initial set (min(x, Mx), Bellman-Ford).  dX holds the start
+ * and receives the fixpoint; dY is scratch of the same shape.  Each iteration
+ * is one (graph-replayed) multiply and one merge kernel that flags changes;
+ * stops when an iteration changes nothing (it is counted) or after max_iters.
+ * *iters = iterations run.  Synchronous on `stream`.  No counterpart function
+ * in the reference, whose semiring sweeps are the single steps of these
+ * iterations. */
+int gmr_engine_fixpoint(gmr_engine* e, int semiring, void* dX, void* dY, int B, int max_iters,
+                        void* stream, int* iters);
+
 /* Several engines in one launch: grammars of uneven size, each with its own
  * semiring, X, Y and B, multiplied by one CUDA-graph launch that runs one
  * branch per engine concurrently (each branch = that engine's AUTO chain).

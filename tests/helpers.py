@@ -76,3 +76,74 @@ def interp_plan(plan, semiring: int, x: np.ndarray) -> np.ndarray:
             else:
                 np.minimum.at(y, row[e0:e1], v)
     return y
+
+
+def brute_left(codes, V, X, rows, cols, semiring):
+    """y = x^T M from the CSRV string (codes val*cols+col+1, 0 = row end), per column of X [rows][B]."""
+    X = np.asarray(X, dtype=np.float64)
+    B = X.shape[1]
+    ends = np.flatnonzero(codes == 0)
+    r = np.repeat(np.arange(len(ends)), np.diff(np.concatenate([[-1], ends])) - 1)
+    nz = codes[codes != 0].astype(np.int64) - 1
+    c, v = nz % cols, np.asarray(V, dtype=np.float64)[nz // cols]
+    if semiring == 0:
+        Y = np.zeros((cols, B))
+        np.add.at(Y, c, v[:, None] * X[r])
+        return Y
+    if semiring == 1:
+        Y = np.zeros((cols, B), dtype=np.int64)
+        np.bitwise_or.at(Y, c, ((v[:, None] != 0) & (X[r] != 0)).astype(np.int64))
+        return Y
+    iv = np.trunc(v).astype(np.int64)[:, None]
+    ix = np.trunc(np.minimum(X[r], 2**31 - 1)).astype(np.int64)
+    leaf = np.where((iv >= INF) | (ix >= INF), INF, iv + ix)
+    Y = np.full((cols, B), INF, dtype=np.int64)
+    np.minimum.at(Y, c, leaf)
+    return Y
+
+
+def interp_left(plan, semiring, X):
+    """FP64 / int evaluation of the left product from the plan's transpose arrays."""
+    s = plan.stats
+    n = s["n_ops"]
+    lvl = plan.array("lvl_off")
+    po, ps = plan.array("par_off"), plan.array("par_src")
+    eo, er = plan.array("erow_off"), plan.array("erow_row")
+    to, tq = plan.array("tcol_off"), plan.array("tcol_q")
+    tv, V, op_c = plan.array("term_val"), plan.array("V"), plan.array("op_c")
+    X = np.asarray(X, dtype=np.float64)
+    B = X.shape[1]
+    zero = {0: 0.0, 1: 0, 2: INF}[semiring]
+    op = {0: np.add, 1: np.bitwise_or, 2: np.minimum}[semiring]
+    dt = np.float64 if semiring == 0 else np.int64
+    Xs = X if semiring == 0 else (X != 0).astype(np.int64) if semiring == 1 else np.minimum(X, INF).astype(np.int64)
+    down = np.full((n, B), zero, dtype=dt)
+
+    def node_down(u):
+        acc = np.full(B, zero, dtype=dt)
+        for p in ps[po[u]:po[u + 1]]:
+            pp = p if p >= 0 else ~p
+            v = down[pp]
+            if semiring == 0 and len(op_c) and p >= 0:
+                v = v * op_c[pp]
+            acc = op(acc, v)
+        for r in er[eo[u]:eo[u + 1]]:
+            acc = op(acc, Xs[r])
+        return acc
+
+    for k in range(s["depth"], 0, -1):
+        for u in range(lvl[k - 1], lvl[k]):
+            down[u] = node_down(u)
+    Y = np.full((s["cols"], B), zero, dtype=dt)
+    for c in range(s["cols"]):
+        for q in tq[to[c]:to[c + 1]]:
+            d = node_down(n + q)
+            v = V[tv[q - 1]]
+            if semiring == 0:
+                l = v * d
+            elif semiring == 1:
+                l = d if v != 0 else np.zeros(B, dtype=dt)
+            else:
+                l = np.where((int(v) >= INF) | (d >= INF), INF, int(v) + d)
+            Y[c] = op(Y[c], l)
+    return Y

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import gmr
-from helpers import INF, SEMIRINGS, golden_cases, golden_meta, load_case
+from helpers import INF, SEMIRINGS, brute_left, golden_cases, golden_meta, load_case
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -268,6 +268,62 @@ def test_allocation_failure_is_reported():
     sched = O.RefSchedule(int(c["alpha"]), c["rules"], c["C"])
     X = random_X(0, 64, 4, 1)
     check(0, eng.multiply(X, 0, B=4), oracle_columns(sched, 0, c["V"], X, 300, 64))
+
+
+@pytest.mark.parametrize("name,sr", [("graph_400", 1), ("graph_w300", 2), ("graph_400", 2)])
+def test_fixpoint_reachability_and_distances(name, sr):
+    """x <- x (+) M x to the fixpoint on the device == the same iteration with the
+    oracle's restatement of the reference sweep, bit for bit."""
+    torch = pytest.importorskip("torch")
+    c = load_case(name)
+    n = int(c["rows"])
+    g = gmr.Grammar.from_arrays(int(c["alpha"]), c["rules"], c["C"], c["V"])
+    eng = gmr.Engine(gmr.Plan.build(g, n, n))
+    sched = O.RefSchedule(int(c["alpha"]), c["rules"], c["C"])
+    rng = np.random.default_rng(sr)
+    B = 40 if sr == 1 else 3
+    if sr == 1:
+        X = (rng.random((n, B)) < 0.01).astype(np.float32)
+    else:
+        X = np.full((n, B), 1e9, dtype=np.float32)
+        X[rng.random((n, B)) < 0.01] = 0.0
+    ref = X.copy()
+    iters_ref = 0
+    while True:
+        iters_ref += 1
+        Y = oracle_columns(sched, sr, c["V"], ref, n, n)
+        new = np.maximum(ref, Y) if sr == 1 else np.minimum(ref, Y)
+        if np.array_equal(new, ref):
+            break
+        ref = new
+    Xw = engine_inputs(sr, X) if sr == 1 else X.astype(np.int32)  # +inf as 1e9, like the oracle
+    dX = torch.from_numpy(Xw.view(np.int32)).cuda()
+    dY = torch.empty_like(dX)
+    it = eng.fixpoint_device(sr, dX.data_ptr(), dY.data_ptr(), B)
+    out = engine_outputs(sr, dX.cpu().numpy().view(np.uint32 if sr == 1 else np.int32), B)
+    assert it == iters_ref
+    check(sr, out, ref)
+
+
+@pytest.mark.parametrize("sr", range(3))
+@pytest.mark.parametrize("B", [1, 8, 33])
+def test_left_product(case, sr, B):
+    """y = x^T M on the GPU against the brute-force transpose product of the expanded matrix."""
+    torch = pytest.importorskip("torch")
+    rows, cols = int(case["rows"]), int(case["cols"])
+    g = gmr.Grammar.from_arrays(int(case["alpha"]), case["rules"], case["C"], case["V"])
+    eng = gmr.Engine(case["plan"])
+    eng.enable_left(case["plan"])
+    X = random_X(sr, rows, B, 900 + B)
+    ref = brute_left(O.expand(g.alpha, g.rules(), g.C()), case["V"].astype(np.float32), X, rows, cols, sr)
+    Xw = engine_inputs(sr, X)
+    dX = torch.from_numpy(Xw.view(np.int32)).cuda()
+    dY = torch.zeros((cols, Xw.shape[1]), dtype=torch.int32, device="cuda")
+    for _ in range(2):
+        eng.multiply_left_device(sr, dX.data_ptr(), dY.data_ptr(), B)
+    torch.cuda.synchronize()
+    Y = engine_outputs(sr, dY.cpu().numpy().view({0: np.float32, 1: np.uint32, 2: np.int32}[sr]), B)
+    check(sr, Y, ref)
 
 
 def test_unittest_grammar_runlength():

@@ -3,7 +3,7 @@ import numpy as np
 import pytest
 
 import gmr
-from helpers import INF, SEMIRINGS, golden_cases, interp_plan, load_case
+from helpers import INF, SEMIRINGS, brute_left, golden_cases, interp_left, interp_plan, load_case
 from oracle import oracle as O
 
 
@@ -256,3 +256,29 @@ def test_alg_bytes_formula(case):
         want = 12 * n_lay + 8 * n_em + 8 * n_te + 8 * (alpha - 1) + 4 * nv + 4 * cols * B + 4 * rows * B
         assert p.alg_bytes(0, B) == want
     assert p.alg_bytes(1, 64) == 12 * n_lay + 8 * n_em + 8 * n_te + 8 * (alpha - 1) + 4 * nv + 8 * cols + 8 * rows
+
+
+@pytest.mark.parametrize("sr", range(3))
+def test_left_product_structures(case, sr):
+    """The transpose arrays, evaluated top-down, give y = x^T M of the expanded matrix."""
+    g = gmr.Grammar.from_arrays(int(case["alpha"]), case["rules"], case["C"], case["V"])
+    rows, cols = int(case["rows"]), int(case["cols"])
+    p = gmr.Plan.build(g, rows, cols)
+    p.prepare_left()
+    assert len(p.array("par_src")) == 2 * p.stats["n_ops"]
+    assert p.array("erow_off")[-1] == p.stats["n_emit"] + p.stats["n_term_emit"]
+    rng = np.random.default_rng(sr)
+    if sr == 0:
+        X = rng.uniform(-1, 1, (rows, 3))
+    elif sr == 1:
+        X = (rng.random((rows, 3)) < 0.3).astype(np.float64)
+    else:
+        X = rng.integers(0, 1000, (rows, 3)).astype(np.float64)
+        X[rng.random(X.shape) < 0.3] = 1e9
+    codes = O.expand(g.alpha, g.rules(), g.C())
+    ref = brute_left(codes, case["V"].astype(np.float32), X, rows, cols, sr)
+    Y = interp_left(p, sr, X)
+    if sr == 0:
+        np.testing.assert_allclose(Y, ref, rtol=1e-6, atol=1e-6)
+    else:
+        np.testing.assert_array_equal(Y, ref)
