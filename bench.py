@@ -542,7 +542,7 @@ def main():
     reps = 5
     lt = np.mean([eng.time_launches(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, variant=args.variant)
                   for _ in range(reps)], axis=0)
-    level_ms = float(lt[1:].sum())       # k_level launches: levels + final fold
+    level_ms = float(lt[1:].sum()) if len(lt) > 1 else float(lt.sum())  # k_level launches (persistent: one)
     if args.dump_launches:
         ops, ems = plan.level_ops(), plan.level_emits()
         log("launch\tms\tops(level k)\temits(level k-1)")

@@ -259,8 +259,8 @@ def test_allocation_failure_is_reported():
     plan = gmr.Plan.build(g, 300, 64)
     eng = gmr.Engine(plan)
     s = plan.stats
-    huge_B = 1 << 27
-    assert (s["n_ops"] + s["n_terms"]) * huge_B * 4 > 400e9  # beyond the device's memory
+    huge_B = 1 << 28
+    assert (s["n_ops"] + s["n_terms"]) * huge_B * 4 > 600e9  # beyond the device's memory (288 GB)
     x = torch.zeros(16, dtype=torch.float32, device="cuda")
     with pytest.raises(gmr.GmrError) as e:
         eng.multiply_device(0, x.data_ptr(), x.data_ptr(), huge_B)
