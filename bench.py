@@ -308,6 +308,50 @@ def timed_loop(torch, stream, fn, n):
     return a.elapsed_time(b) / n
 
 
+def cusparse_baseline(torch, args, rows, cols, B, n=20):
+    """cuSPARSE CSR SpMM (through torch.sparse) on the UNCOMPRESSED matrix of the
+    same workload, fp32, same B: the reference's library baseline
+    (gpu-engine/cusparse_test.cu:432-502).  Reported beside the engine; not the
+    path under test."""
+    import gmr
+
+    if args.workload not in MOSAICS or args.semiring != "plustimes":
+        return None
+    r, c, F, sw, mu, seed = MOSAICS[args.workload]
+    t0 = time.perf_counter()
+    m = gmr.gen_mosaic(r, c, F, sw, mu, seed)
+    codes = m.codes()
+    del m
+    ends = np.flatnonzero(codes == 0)
+    crow = np.zeros(rows + 1, dtype=np.int64)
+    crow[1:len(ends) + 1] = ends - np.arange(len(ends))
+    crow[len(ends) + 1:] = crow[len(ends)]
+    colv = (codes[codes != 0] - 1).astype(np.int32)  # value index 0: every stored value is 1
+    del codes
+    nnz = int(colv.size)
+    try:
+        A = torch.sparse_csr_tensor(torch.from_numpy(crow).cuda(), torch.from_numpy(colv).to(torch.int64).cuda(),
+                                    torch.ones(nnz, device="cuda"), size=(rows, cols))
+    except RuntimeError as e:  # out of memory or unsupported
+        return {"unavailable": str(e).splitlines()[0]}
+    build_s = time.perf_counter() - t0
+    X = torch.rand((cols, B), device="cuda") * 2 - 1
+    stream = torch.cuda.current_stream()
+    for _ in range(3):
+        Yc = A @ X
+    ms = timed_loop(torch, stream, lambda: A @ X, n)
+    x1 = X[:, :1].contiguous()
+    for _ in range(3):
+        A @ x1
+    ms1 = timed_loop(torch, stream, lambda: A @ x1, n)
+    out = {"spmm_vps": B * 1000.0 / ms, "spmm_ms": ms, "spmv_vps": 1000.0 / ms1, "nnz": nnz,
+           "csr_bytes": int(nnz * 8 + (rows + 1) * 8), "build_s": round(build_s, 1),
+           "how": "torch.sparse_csr_tensor @ dense (cuSPARSE), fp32, int64 indices"}
+    del A, Yc
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_pack8(args):
     """Eight mosaic grammars of uneven size (rows ~U{5k..200k}, cols ~U{1k..10k},
     seeds 10-17), each with its own B in {1, 4, 16, 64}, in one graph launch."""
@@ -555,6 +599,13 @@ def main():
     alg_level = alg_total - alg_pro      # 12 N_L + 8 E + 8 E_T
     peak, peak_kind = measured_peak_hbm()
     achieved = alg_level / (level_ms / 1000.0) / 1e9
+    # value traffic the sweep must move at this B (every emission gathers one
+    # value, every rule reads two and writes one), against the measured ceilings
+    # of random 128-byte gathers from L2 and from HBM on this GPU
+    vbytes = 4.0 * words * (st["n_emit"] + st["n_term_emit"] + 3 * st["n_ops"])
+    ceil_l2 = gmr.measure_gather_bandwidth(64 << 20, device=local)
+    ceil_hbm = gmr.measure_gather_bandwidth(4 << 30, device=local)
+    value_gbs = vbytes / (level_ms / 1000.0) / 1e9
     step_gbs = alg_total / (ms_per_step / 1000.0) / 1e9
     traffic = None
     tf = REPO / "profiles" / "traffic.json"
@@ -601,7 +652,10 @@ def main():
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": "k_level (all level launches of one multiply)",
                      "alg_bytes_per_multiply": alg_level, "kernel_ms_per_multiply": level_ms,
-                     "step_alg_gbs": step_gbs},
+                     "step_alg_gbs": step_gbs,
+                     "gather_ceiling": {"value_bytes_per_multiply": vbytes, "achieved_gbs": value_gbs,
+                                        "l2_random_128B_gbs": ceil_l2, "hbm_random_128B_gbs": ceil_hbm,
+                                        "frac_of_l2_ceiling": value_gbs / ceil_l2}},
         "e2e": {"value": e2e_value, "unit": "vectors/s", "h2d_bytes_per_step": int(cols * words * 4),
                 "d2h_bytes_per_step": int(rows * words * 4)},
         "gpu_launches": int(launches_per_step * args.steps),

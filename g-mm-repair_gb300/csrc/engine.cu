@@ -1705,6 +1705,78 @@ extern "C" void gmr_pack_free(gmr_pack* p) {
     delete p;
 }
 
+// ------------------------------------------------------------------ gather-bandwidth calibration
+// The sweep's dominant kernel gathers whole 128-byte values at data-dependent
+// addresses; its ceiling is the random-line gather bandwidth of the GPU, from
+// L2 (working set that fits) and from HBM (one that does not).  This
+// calibration measures both with the same access pattern (indices taken
+// modulo the buffer's line count, so every access is in bounds).
+namespace gmr {
+
+__device__ __forceinline__ unsigned mix32(unsigned x) {
+    x ^= x >> 16;
+    x *= 0x7feb352dU;
+    x ^= x >> 15;
+    x *= 0x846ca68bU;
+    x ^= x >> 16;
+    return x;
+}
+
+__global__ void __launch_bounds__(256) k_gather_lines(const float4* __restrict__ buf, unsigned nlines, int64_t items,
+                                                      float* __restrict__ sink) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    float acc = 0.0f;
+    for (int64_t i = t; i < items * 8; i += 4 * stride) {
+        float4 v[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int64_t ii = i + j * stride;
+            const unsigned line = mix32((unsigned)(ii >> 3)) % nlines;
+            v[j] = ii < items * 8 ? __ldg(buf + (int64_t)line * 8 + (ii & 7)) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc += v[j].x + v[j].y + v[j].z + v[j].w;
+    }
+    if (acc == 1.2345f) sink[t & 255] = acc;  // keeps the loads
+}
+
+}  // namespace gmr
+
+extern "C" int gmr_measure_gather_bandwidth(int device, int64_t buffer_bytes, float* gbs) {
+    return guarded([&] {
+        if (!gbs || buffer_bytes < 4096 || buffer_bytes > (int64_t)64 << 30) throw Error(GMR_ERR_ARG, "bad argument");
+        DeviceGuard dg(device);
+        const int64_t lines = buffer_bytes / 128;
+        DevBuf buf, sink;
+        buf.ensure((size_t)lines * 128);
+        sink.ensure(1024);
+        GMR_CUDA(cudaMemset(buf.p, 0, (size_t)lines * 128));
+        int sms = 152;
+        GMR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+        const int64_t items = 50000000;  // 128-byte lines gathered per timed run
+        cudaEvent_t a, b;
+        GMR_CUDA(cudaEventCreate(&a));
+        GMR_CUDA(cudaEventCreate(&b));
+        k_gather_lines<<<sms * 16, 256>>>(static_cast<const float4*>(buf.p), (unsigned)lines, items / 10,
+                                          static_cast<float*>(sink.p));
+        float best = 0.0f;
+        for (int r = 0; r < 3; ++r) {
+            cudaEventRecord(a);
+            k_gather_lines<<<sms * 16, 256>>>(static_cast<const float4*>(buf.p), (unsigned)lines, items,
+                                              static_cast<float*>(sink.p));
+            cudaEventRecord(b);
+            GMR_CUDA(cudaEventSynchronize(b));
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, a, b);
+            best = std::max(best, (float)(items * 128.0 / (ms * 1e6)));
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        GMR_CUDA(cudaGetLastError());
+        *gbs = best;
+    });
+}
+
 // ------------------------------------------------------------------ no-allocation entry point
 // For callers that may not allocate device memory while they run: the
 // scratch values live in this statically sized device array instead of

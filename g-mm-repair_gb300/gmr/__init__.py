@@ -531,6 +531,13 @@ class Pack:
         self.close()
 
 
+def measure_gather_bandwidth(buffer_bytes: int, device: int = 0) -> float:
+    """Random 128-byte line gather bandwidth (GB/s) over a buffer of that size."""
+    g = C.c_float()
+    _check(lib().gmr_measure_gather_bandwidth(device, int(buffer_bytes), C.byref(g)))
+    return float(g.value)
+
+
 # ---------------------------------------------------------------- legacy ABI
 def _legacy_args(rows, cols, alpha, rules_lrc, val_indices, col_indices, V, sched):
     keep = []
