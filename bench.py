@@ -506,9 +506,22 @@ def main():
     g, rows, cols, ginfo = workload_grammar(args)
     if ws > 1 and rank == 0:
         torch.distributed.barrier()
+    # schedule: built on the GPU (timed on a second build, after the first
+    # loaded the kernels), checked array for array against the host build
     t0 = time.perf_counter()
-    plan = gmr.Plan.build(g, rows, cols)
+    plan = gmr.Plan.build(g, rows, cols, device=local)
+    plan_dev_first_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    plan = gmr.Plan.build(g, rows, cols, device=local)
+    plan_dev_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    plan_host = gmr.Plan.build(g, rows, cols)
     plan_s = time.perf_counter() - t0
+    plan_same = plan_host.stats == plan.stats and all(
+        np.array_equal(plan.array(a), plan_host.array(a)) for a in
+        ("op_l", "op_r", "op_c", "lvl_off", "em_off", "em_src", "em_row", "term_val", "term_col", "seg_off",
+         "seg_row", "seg_start"))
+    del plan_host
     st = plan.stats
     eng = gmr.Engine(plan, device=local)
     sr = SR_IDS[args.semiring]
@@ -664,7 +677,8 @@ def main():
         "grammar": {"ops": st["n_ops"], "depth": st["depth"], "layered_rules": st["ref_layered"],
                     "passthrough": st["ref_passthrough"], "max_width": st["ref_max_width"],
                     "emit": st["ref_emit"], "term_emit": st["ref_term_emit"], "terminals": st["ref_alpha"],
-                    "plan_s": round(plan_s, 2)} | ginfo,
+                    "plan_s": round(plan_s, 2), "plan_device_s": round(plan_dev_s, 3),
+                    "plan_device_first_s": round(plan_dev_first_s, 3), "plan_device_identical": plan_same} | ginfo,
     }
     if rank == 0 and ws == 1 and not args.no_cusparse:
         del eng  # free the engine's device memory before building the CSR baseline

@@ -38,15 +38,9 @@
 #include <vector>
 
 #include "gmr_internal.h"
+#include "device_util.cuh"
 
 namespace gmr {
-
-#define GMR_CUDA(call)                                                                                  \
-    do {                                                                                                \
-        cudaError_t err_ = (call);                                                                      \
-        if (err_ != cudaSuccess)                                                                        \
-            throw ::gmr::Error(GMR_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(err_));    \
-    } while (0)
 
 // ------------------------------------------------------------------ semirings
 struct SPlus {
@@ -551,36 +545,6 @@ __global__ void __launch_bounds__(256) k_persistent(SweepArgs a, LevelArgs L0, P
 }
 
 // ------------------------------------------------------------------ engine
-struct DevBuf {
-    void* p = nullptr;
-    size_t bytes = 0;
-    void ensure(size_t n) {
-        if (n <= bytes) return;
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-        cudaError_t e = cudaMalloc(&p, n ? n : 16);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            throw Error(e == cudaErrorMemoryAllocation ? GMR_ERR_OOM : GMR_ERR_CUDA,
-                        std::string("cudaMalloc(") + std::to_string(n) + "): " + cudaGetErrorString(e));
-        }
-        bytes = n;
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        bytes = 0;
-    }
-};
-
-template <class T>
-static T* upload(const std::vector<T>& h, DevBuf& b) {
-    b.ensure(h.size() * sizeof(T));
-    if (!h.empty()) GMR_CUDA(cudaMemcpy(b.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
-    return static_cast<T*>(b.p);
-}
-
 // Fully resolved launch configuration of one multiply.
 // Kernel variants a k_level launch can use: emission folding strategy and
 // chunk, and how many CTAs evaluate the level's rules (few CTAs = many
@@ -656,18 +620,6 @@ struct gmr_engine {
 
 namespace gmr {
 
-struct DeviceGuard {
-    int prev = -1;
-    explicit DeviceGuard(int dev) {
-        cudaGetDevice(&prev);
-        if (prev != dev) GMR_CUDA(cudaSetDevice(dev));
-    }
-    ~DeviceGuard() {
-        int cur = -1;
-        cudaGetDevice(&cur);
-        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
-    }
-};
 
 static int words_per_slot(int semiring, int B) { return semiring == GMR_BOOLEAN ? (B + 31) / 32 : B; }
 

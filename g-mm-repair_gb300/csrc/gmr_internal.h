@@ -103,6 +103,7 @@ struct gmr_plan {
 
 namespace gmr {
 void validate_plan(const gmr_plan& p);  // throws Error(GMR_ERR_FORMAT)
+void fill_common_stats(gmr_plan& p);    // stats derived from the plan arrays
 }
 
 #include <thread>

@@ -121,6 +121,8 @@ void build_segments(gmr_plan& p) {
     p.seg_start.push_back((int64_t)p.em_src.size());
 }
 
+}  // namespace
+
 void fill_common_stats(gmr_plan& p) {
     auto& s = p.stats;
     s.rows = p.rows;
@@ -136,8 +138,6 @@ void fill_common_stats(gmr_plan& p) {
     for (int k = 1; k <= p.depth; ++k) mx = std::max(mx, p.lvl_off[k] - p.lvl_off[k - 1]);
     s.max_level_ops = mx;
 }
-
-}  // namespace
 
 void validate_plan(const gmr_plan& p) {
     const int D = p.depth;

@@ -266,9 +266,14 @@ class Plan:
             self._h = C.c_void_p()
 
     @classmethod
-    def build(cls, g: Grammar, rows: int, cols: int) -> "Plan":
+    def build(cls, g: Grammar, rows: int, cols: int, device: int | None = None, validate: bool = False) -> "Plan":
+        """Level-major plan of a grammar.  device=None builds on the host;
+        device=d builds the identical plan on GPU d."""
         h = C.c_void_p()
-        _check(lib().gmr_plan_build(g._h, rows, cols, C.byref(h)))
+        if device is None:
+            _check(lib().gmr_plan_build(g._h, rows, cols, C.byref(h)))
+        else:
+            _check(lib().gmr_plan_build_device(g._h, rows, cols, int(device), int(bool(validate)), C.byref(h)))
         return cls(h)
 
     @classmethod

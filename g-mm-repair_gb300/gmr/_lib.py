@@ -96,6 +96,7 @@ _SIGS = {
     "gmr_gen_copy_graph": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_int, C.c_uint64, C.c_int, C.POINTER(P)]),
     "gmr_repair_compress": (C.c_int, [P, C.c_int, C.POINTER(P)]),
     "gmr_plan_build": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(P)]),
+    "gmr_plan_build_device": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(P)]),
     "gmr_plan_from_layered": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(LayeredRule), I32P, I32P,
                                         F32P, C.c_int, C.POINTER(GPUSchedule), C.POINTER(P)]),
     "gmr_plan_get_stats": (C.c_int, [P, C.POINTER(PlanStats)]),

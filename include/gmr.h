@@ -181,6 +181,12 @@ typedef struct {
 } gmr_plan_stats;
 
 int gmr_plan_build(const gmr_grammar* g, int rows, int cols, gmr_plan** out);
+/* The same plan as gmr_plan_build (identical arrays and figures, same errors),
+ * built on GPU `device`: replaces the host build_schedule()
+ * (build_schedule.cpp:42-227).  validate != 0 also runs the host-side plan
+ * check.  Allocates device memory for the build and frees it on return. */
+int gmr_plan_build_device(const gmr_grammar* g, int rows, int cols, int device, int validate,
+                          gmr_plan** out);
 int gmr_plan_from_layered(int rows, int cols, int alpha, int total_layered_rules,
                           const LayeredRule* rules, const int* val_indices,
                           const int* col_indices, const float* V, int n_vals,
