@@ -600,8 +600,10 @@ struct gmr_engine {
     gmr::DevBuf em_src_c, em_row_c, seg_row_c, seg_start_c;
     std::vector<int64_t> ch_off, ch_em, ch_seg;
     bool chunked = false;
-    // Left product (y = x^T M): reverse adjacency uploaded by gmr_engine_enable_left.
-    gmr::DevBuf par_off, par_src, erow_off, erow_row, tcol_off, tcol_q;
+    // Left product (y = x^T M): flat edge lists uploaded by gmr_engine_enable_left.
+    gmr::DevBuf le_src, le_tgt, le_split, tcol_off, tcol_q;
+    std::vector<int64_t> le_off;
+    int64_t n_left_split = 0;
     bool left_ready = false;
     int* status_host = nullptr;                           // pinned copy of the last persistent error words
     bool last_persistent = false;
@@ -614,7 +616,7 @@ struct gmr_engine {
     std::vector<gmr::DevBuf*> schedule_bufs() {
         return {&ops, &op_c, &em_src, &em_row, &seg_row, &seg_start, &term_val, &term_col, &V,
                 &d_lvl_off, &d_em_off, &d_seg_off, &sync, &em_src_c, &em_row_c, &seg_row_c, &seg_start_c,
-                &par_off, &par_src, &erow_off, &erow_row, &tcol_off, &tcol_q};
+                &le_src, &le_tgt, &le_split, &tcol_off, &tcol_q};
     }
 };
 
@@ -1319,16 +1321,23 @@ extern "C" void gmr_engine_free(gmr_engine* e) {
 // the run-length coefficient for a left child) and of x over the rows that
 // emit it; levels run from the top down (a parent is always above its
 // children), then every column folds leaf(V, down) over its terminals.
+//
+// Each level is one launch over its flat edge list (targets ascending): a lane
+// group folds a chunk of kLeftChunk edges in registers and writes a target
+// whose edges all lie in the chunk with a plain store; a target whose edges
+// straddle chunks was set to the semiring zero before the first level and
+// each chunk folds its part into it atomically.  Symbols with thousands of
+// parents or rows are thereby spread over many lane groups.
 namespace gmr {
 
 struct LeftArgs {
-    void* down;  // [n_ops][Bw] (the arena)
+    void* down;     // [n_ops][Bw] (the arena): rules' down values
+    void* tdown;    // [U][Bw] (the terminal table): terminals' down values
     const void* X;  // [rows][Bw]
     void* Y;        // [cols][Bw]
-    const int64_t* par_off;
-    const int32_t* par_src;
-    const int64_t* erow_off;
-    const int32_t* erow_row;
+    const int32_t* src;
+    const int32_t* tgt;
+    const int32_t* split;
     const int64_t* tcol_off;
     const int32_t* tcol_q;
     const float* op_c;
@@ -1336,38 +1345,97 @@ struct LeftArgs {
     const int32_t* term_val;
     int64_t n_ops, first, count;
     int Bw, G;
+    bool terminals;  // targets of this launch are terminals (tdown) rather than rules (down)
 };
 
-template <class S, int VEC, int GLOG>
-__device__ __forceinline__ Vec<typename S::T, VEC> left_down(const LeftArgs& a, int64_t u, int lane) {
+template <class S, int VEC>
+__device__ __forceinline__ Vec<typename S::T, VEC> left_edge_value(const LeftArgs& a, int32_t s, int lane) {
     using T = typename S::T;
-    Vec<T, VEC> acc = vzero<S, VEC>();
-    const T* down = static_cast<const T*>(a.down);
-    for (int64_t e = __ldg(a.par_off + u), e1 = __ldg(a.par_off + u + 1); e < e1; ++e) {
-        const int32_t p = __ldg(a.par_src + e);
-        const int64_t pp = p >= 0 ? p : ~p;
-        Vec<T, VEC> v = vload_rw<T, VEC>(down + pp * a.Bw + lane * VEC);
-        if (a.op_c && p >= 0) {
-            const float c = __ldg(a.op_c + pp);
+    const bool row = (int64_t)s >= a.n_ops;
+    const int64_t pp = s >= 0 ? (int64_t)s : (int64_t)~s;
+    const T* base = row ? static_cast<const T*>(a.X) + (pp - a.n_ops) * a.Bw : static_cast<const T*>(a.down) + pp * a.Bw;
+    Vec<T, VEC> v = vload<T, VEC>(base + lane * VEC);
+    if (a.op_c && s >= 0 && !row) {
+        const float c = __ldg(a.op_c + pp);
 #pragma unroll
-            for (int j = 0; j < VEC; ++j) v.v[j] = S::apply(v.v[j], c);
-        }
-        acc = voplus<S, VEC>(acc, v);
+        for (int j = 0; j < VEC; ++j) v.v[j] = S::apply(v.v[j], c);
     }
-    const T* X = static_cast<const T*>(a.X);
-    for (int64_t e = __ldg(a.erow_off + u), e1 = __ldg(a.erow_off + u + 1); e < e1; ++e)
-        acc = voplus<S, VEC>(acc, vload<T, VEC>(X + (int64_t)__ldg(a.erow_row + e) * a.Bw + lane * VEC));
-    return acc;
+    return v;
+}
+
+template <class S, int VEC>
+__device__ __forceinline__ void left_flush(const LeftArgs& a, int32_t u, int lane, bool whole,
+                                           const Vec<typename S::T, VEC>& acc) {
+    using T = typename S::T;
+    T* p = static_cast<T*>(a.terminals ? a.tdown : a.down) + (int64_t)u * a.Bw + lane * VEC;
+    if (whole) vstore<T, VEC>(p, acc);
+    else vred<S, VEC>(p, acc);
+}
+
+// Straddling targets start at the semiring zero.
+template <class S, int VEC, int GLOG>
+__global__ void __launch_bounds__(256) k_left_zero(LeftArgs a) {
+    using T = typename S::T;
+    const int64_t items = items_of<GLOG>(a.count, a.G);  // count = straddling targets
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < items; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t u = __ldg(a.split + unit_of<GLOG>(t, a.G));
+        const int lane = lane_of<GLOG>(t, a.G);
+        T* p = u < a.n_ops ? static_cast<T*>(a.down) + u * a.Bw : static_cast<T*>(a.tdown) + (u - a.n_ops) * a.Bw;
+        vstore<T, VEC>(p + lane * VEC, vzero<S, VEC>());
+    }
 }
 
 template <class S, int VEC, int GLOG>
-__global__ void __launch_bounds__(256) k_left_level(LeftArgs a) {
+__global__ void __launch_bounds__(256) k_left_fold(LeftArgs a) {
     using T = typename S::T;
-    const int64_t items = items_of<GLOG>(a.count, a.G);
+    const int64_t groups = (a.count + kLeftChunk - 1) / kLeftChunk;
+    const int64_t items = items_of<GLOG>(groups, a.G);
+    const int32_t* src = a.src + a.first;
+    const int32_t* tgt = a.tgt + a.first;
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < items; t += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t u = a.first + unit_of<GLOG>(t, a.G);
+        const int64_t g = unit_of<GLOG>(t, a.G);
         const int lane = lane_of<GLOG>(t, a.G);
-        vstore<T, VEC>(static_cast<T*>(a.down) + u * a.Bw + lane * VEC, left_down<S, VEC, GLOG>(a, u, lane));
+        const int64_t e0 = g * kLeftChunk, e1 = min(e0 + kLeftChunk, a.count);
+        int32_t cur = __ldg(tgt + e0);
+        bool whole = e0 == 0 || __ldg(tgt + e0 - 1) != cur;  // cur's first edge is in this chunk
+        Vec<T, VEC> acc = vzero<S, VEC>();
+        int64_t e = e0;
+        for (; e + 4 <= e1; e += 4) {
+            int32_t u[4], s4[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                u[j] = __ldg(tgt + e + j);
+                s4[j] = __ldg(src + e + j);
+            }
+            Vec<T, VEC> v[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) v[j] = left_edge_value<S, VEC>(a, s4[j], lane);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (u[j] != cur) {
+                    left_flush<S, VEC>(a, cur, lane, whole, acc);
+                    whole = true;
+                    acc = v[j];
+                    cur = u[j];
+                } else {
+                    acc = voplus<S, VEC>(acc, v[j]);
+                }
+            }
+        }
+        for (; e < e1; ++e) {
+            const int32_t u = __ldg(tgt + e);
+            const Vec<T, VEC> v = left_edge_value<S, VEC>(a, __ldg(src + e), lane);
+            if (u != cur) {
+                left_flush<S, VEC>(a, cur, lane, whole, acc);
+                whole = true;
+                acc = v;
+                cur = u;
+            } else {
+                acc = voplus<S, VEC>(acc, v);
+            }
+        }
+        const bool ends = e1 == a.count || __ldg(tgt + e1) != cur;  // cur's last edge is in this chunk
+        left_flush<S, VEC>(a, cur, lane, whole && ends, acc);
     }
 }
 
@@ -1375,13 +1443,14 @@ template <class S, int VEC, int GLOG>
 __global__ void __launch_bounds__(256) k_left_columns(LeftArgs a) {
     using T = typename S::T;
     const int64_t items = items_of<GLOG>(a.count, a.G);  // count = cols
+    const T* tdown = static_cast<const T*>(a.tdown);
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < items; t += (int64_t)gridDim.x * blockDim.x) {
         const int64_t c = unit_of<GLOG>(t, a.G);
         const int lane = lane_of<GLOG>(t, a.G);
         Vec<T, VEC> acc = vzero<S, VEC>();
         for (int64_t i = __ldg(a.tcol_off + c), i1 = __ldg(a.tcol_off + c + 1); i < i1; ++i) {
             const int32_t q = __ldg(a.tcol_q + i);
-            const Vec<T, VEC> d = left_down<S, VEC, GLOG>(a, a.n_ops + q, lane);
+            const Vec<T, VEC> d = vload<T, VEC>(tdown + (int64_t)q * a.Bw + lane * VEC);
             const float v = __ldg(a.V + __ldg(a.term_val + q - 1));
             Vec<T, VEC> l;
 #pragma unroll
@@ -1396,12 +1465,12 @@ template <class S, int VEC, int GLOG>
 static void left_chain_t(gmr_engine* e, int Bw, int G, const void* X, void* Y, cudaStream_t st) {
     LeftArgs a{};
     a.down = e->arena.p;
+    a.tdown = e->T.p;
     a.X = X;
     a.Y = Y;
-    a.par_off = static_cast<const int64_t*>(e->par_off.p);
-    a.par_src = static_cast<const int32_t*>(e->par_src.p);
-    a.erow_off = static_cast<const int64_t*>(e->erow_off.p);
-    a.erow_row = static_cast<const int32_t*>(e->erow_row.p);
+    a.src = static_cast<const int32_t*>(e->le_src.p);
+    a.tgt = static_cast<const int32_t*>(e->le_tgt.p);
+    a.split = static_cast<const int32_t*>(e->le_split.p);
     a.tcol_off = static_cast<const int64_t*>(e->tcol_off.p);
     a.tcol_q = static_cast<const int32_t*>(e->tcol_q.p);
     a.op_c = e->has_coeff ? static_cast<const float*>(e->op_c.p) : nullptr;
@@ -1413,11 +1482,16 @@ static void left_chain_t(gmr_engine* e, int Bw, int G, const void* X, void* Y, c
     auto blocks = [&](int64_t items) {
         return (int)std::max<int64_t>(1, std::min<int64_t>((items + 255) / 256, (int64_t)e->sm_count * 32));
     };
-    for (int k = e->depth; k >= 1; --k) {
-        a.first = e->lvl_off[k - 1];
-        a.count = e->lvl_off[k] - e->lvl_off[k - 1];
+    const int D = e->depth;
+    a.count = e->n_left_split;
+    if (a.count) k_left_zero<S, VEC, GLOG><<<blocks(a.count * G), 256, 0, st>>>(a);
+    for (int j = D; j >= 0; --j) {  // levels D .. 1 from the top, then the terminals (range D + 1)
+        const int k = j ? j : D + 1;
+        a.first = e->le_off[k - 1];
+        a.count = e->le_off[k] - e->le_off[k - 1];
+        a.terminals = k == D + 1;
         if (a.count == 0) continue;
-        k_left_level<S, VEC, GLOG><<<blocks(a.count * G), 256, 0, st>>>(a);
+        k_left_fold<S, VEC, GLOG><<<blocks((a.count + kLeftChunk - 1) / kLeftChunk * G), 256, 0, st>>>(a);
     }
     a.first = 0;
     a.count = e->cols;
@@ -1454,12 +1528,13 @@ extern "C" int gmr_engine_enable_left(gmr_engine* e, gmr_plan* p) {
         if (rc != GMR_OK) throw Error(rc, gmr_last_error());
         std::lock_guard<std::mutex> lk(e->mu);
         DeviceGuard dg(e->device);
-        upload(p->par_off, e->par_off);
-        upload(p->par_src, e->par_src);
-        upload(p->erow_off, e->erow_off);
-        upload(p->erow_row, e->erow_row);
+        upload(p->le_src, e->le_src);
+        upload(p->le_tgt, e->le_tgt);
+        upload(p->le_split, e->le_split);
         upload(p->tcol_off, e->tcol_off);
         upload(p->tcol_q, e->tcol_q);
+        e->le_off = p->le_off;
+        e->n_left_split = (int64_t)p->le_split.size();
         e->left_ready = true;
     });
 }
@@ -1481,7 +1556,7 @@ extern "C" int gmr_engine_multiply_left(gmr_engine* e, int semiring, const void*
         if (semiring == GMR_PLUS_TIMES) left_chain_s<SPlus>(e, Bw, dX, dY, st);
         else if (semiring == GMR_BOOLEAN) left_chain_s<SBool>(e, Bw, dX, dY, st);
         else left_chain_s<STrop>(e, Bw, dX, dY, st);
-        e->last_launches = e->depth + 1;
+        e->last_launches = e->depth + 2 + (e->n_left_split ? 1 : 0);
     });
 }
 

@@ -95,6 +95,17 @@ struct gmr_plan {
     // Terminals of column c: tcol_q[tcol_off[c] .. tcol_off[c+1]) (q >= 1).
     std::vector<int64_t> par_off, erow_off, tcol_off;
     std::vector<int32_t> par_src, erow_row, tcol_q;
+    // The same edges flattened for the chunked left fold: edge e adds source
+    // le_src[e] into target le_tgt[e].  Sources: p >= 0 (down value of parent
+    // p, u its left child, times p's coefficient), ~p (parent p, right child),
+    // n_ops + r (x row r).  Targets: arena slot u (levels 1..depth), or
+    // compacted terminal q (level 0).  Level k's edges are [le_off[k-1],
+    // le_off[k]), terminals' [le_off[depth], le_off[depth+1]); targets are
+    // ascending within each range.  le_split: targets whose edges straddle a
+    // chunk of kLeftChunk edges (counted from the start of their range),
+    // encoded u or n_ops + q; they are folded with atomics into a zeroed value.
+    std::vector<int64_t> le_off;
+    std::vector<int32_t> le_src, le_tgt, le_split;
 
     int64_t n_ops() const { return (int64_t)op_l.size(); }
     int64_t n_terms() const { return (int64_t)term_val.size() + 1; }
@@ -102,6 +113,7 @@ struct gmr_plan {
 };
 
 namespace gmr {
+constexpr int64_t kLeftChunk = 16;  // edges per lane group in the left fold
 void validate_plan(const gmr_plan& p);  // throws Error(GMR_ERR_FORMAT)
 void fill_common_stats(gmr_plan& p);    // stats derived from the plan arrays
 }

@@ -570,12 +570,50 @@ extern "C" int gmr_plan_prepare_left(gmr_plan* p) {
         }
         for (size_t e = 0; e < p->em_src.size(); ++e) er[fe[node(p->em_src[e])]++] = p->em_row[e];
         for (size_t q = 0; q < p->term_col.size(); ++q) tq[fc[p->term_col[q]]++] = (int32_t)(q + 1);
+        // flat edge lists for the chunked left fold
+        if (n + (int64_t)p->rows > (int64_t)INT32_MAX) throw Error(GMR_ERR_RANGE, "left product: rules + rows exceed 2^31");
+        const int64_t tot = (po[n] - po[0]) + (eo[n] - eo[0]) + (po[N] - po[n + 1]) + (eo[N] - eo[n + 1]);
+        std::vector<int32_t> src((size_t)tot), tgt((size_t)tot);
+        std::vector<int64_t> start((size_t)N + 1, 0);  // first edge of each node
+        int64_t w = 0;
+        auto emit_node = [&](int64_t u, int32_t t) {
+            start[u] = w;
+            for (int64_t j = po[u]; j < po[u + 1]; ++j, ++w) {
+                src[w] = ps[j];
+                tgt[w] = t;
+            }
+            for (int64_t j = eo[u]; j < eo[u + 1]; ++j, ++w) {
+                src[w] = (int32_t)(n + er[j]);
+                tgt[w] = t;
+            }
+        };
+        for (int64_t u = 0; u < n; ++u) emit_node(u, (int32_t)u);
+        for (int64_t q = 1; q < U; ++q) emit_node(n + q, (int32_t)q);
+        const int D = p->depth;
+        std::vector<int64_t> lo((size_t)D + 2, 0);
+        for (int k = 1; k <= D; ++k) lo[k] = p->lvl_off[k] < n ? start[p->lvl_off[k]] : (po[n] - po[0]) + (eo[n] - eo[0]);
+        lo[D + 1] = tot;
+        std::vector<int32_t> split;
+        for (int k = 1; k <= D + 1; ++k) {
+            const int64_t a = lo[k - 1], b = lo[k];
+            for (int64_t e = a; e < b;) {
+                int64_t f = e + 1;
+                while (f < b && tgt[f] == tgt[e]) ++f;
+                if ((e - a) / kLeftChunk != (f - 1 - a) / kLeftChunk)
+                    split.push_back(k <= D ? tgt[e] : (int32_t)(n + tgt[e]));
+                e = f;
+            }
+        }
         p->par_off.swap(po);
         p->erow_off.swap(eo);
         p->tcol_off.swap(co);
         p->par_src.swap(ps);
         p->erow_row.swap(er);
         p->tcol_q.swap(tq);
+        p->le_off.swap(lo);
+        p->le_src.swap(src);
+        p->le_tgt.swap(tgt);
+        p->le_split.swap(split);
     });
 }
 
@@ -661,6 +699,10 @@ extern "C" int gmr_plan_array(const gmr_plan* p, int which, const void** ptr, in
             case 16: *ptr = p->erow_row.data(); *n = (int64_t)p->erow_row.size(); break;
             case 17: *ptr = p->tcol_off.data(); *n = (int64_t)p->tcol_off.size(); break;
             case 18: *ptr = p->tcol_q.data(); *n = (int64_t)p->tcol_q.size(); break;
+            case 19: *ptr = p->le_off.data(); *n = (int64_t)p->le_off.size(); break;
+            case 20: *ptr = p->le_src.data(); *n = (int64_t)p->le_src.size(); break;
+            case 21: *ptr = p->le_tgt.data(); *n = (int64_t)p->le_tgt.size(); break;
+            case 22: *ptr = p->le_split.data(); *n = (int64_t)p->le_split.size(); break;
             default: throw Error(GMR_ERR_ARG, "unknown plan array");
         }
     });

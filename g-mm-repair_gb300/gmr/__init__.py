@@ -318,7 +318,9 @@ class Plan:
                "term_val": (7, np.int32), "term_col": (8, np.int32), "V": (9, np.float32),
                "seg_off": (10, np.int64), "seg_row": (11, np.int32), "seg_start": (12, np.int64),
                "par_off": (13, np.int64), "par_src": (14, np.int32), "erow_off": (15, np.int64),
-               "erow_row": (16, np.int32), "tcol_off": (17, np.int64), "tcol_q": (18, np.int32)}
+               "erow_row": (16, np.int32), "tcol_off": (17, np.int64), "tcol_q": (18, np.int32),
+               "le_off": (19, np.int64), "le_src": (20, np.int32), "le_tgt": (21, np.int32),
+               "le_split": (22, np.int32)}
 
     def array(self, name: str) -> np.ndarray:
         which, dt = self._ARRAYS[name]

@@ -210,7 +210,8 @@ double gmr_plan_alg_bytes(const gmr_plan* p, int semiring, int B);
  * n_seg+1): the emissions of one (level, row) pair form one row segment;
  * after gmr_plan_prepare_left: 13 par_off (int64), 14 par_src (int32),
  * 15 erow_off (int64), 16 erow_row (int32), 17 tcol_off (int64),
- * 18 tcol_q (int32) (see gmr_plan_prepare_left).
+ * 18 tcol_q (int32), 19 le_off (int64, depth+2), 20 le_src (int32),
+ * 21 le_tgt (int32), 22 le_split (int32) (see gmr_plan_prepare_left).
  * *ptr stays valid until gmr_plan_free. */
 int gmr_plan_array(const gmr_plan* p, int which, const void** ptr, int64_t* n);
 /* Human-readable per-level report (the host_scheduler inspector). */

@@ -147,3 +147,57 @@ def interp_left(plan, semiring, X):
                 l = np.where((int(v) >= INF) | (d >= INF), INF, int(v) + d)
             Y[c] = op(Y[c], l)
     return Y
+
+
+def interp_left_edges(plan, semiring, X, chunk=16):
+    """The left product evaluated from the flat edge lists (le_*), level by
+    level from the top, as the chunked fold does; also checks that le_split
+    holds exactly the targets whose edges straddle a chunk."""
+    s = plan.stats
+    n, D = s["n_ops"], s["depth"]
+    lo, src, tgt, split = (plan.array(a) for a in ("le_off", "le_src", "le_tgt", "le_split"))
+    to, tq = plan.array("tcol_off"), plan.array("tcol_q")
+    tv, V, op_c = plan.array("term_val"), plan.array("V"), plan.array("op_c")
+    X = np.asarray(X, dtype=np.float64)
+    B = X.shape[1]
+    zero = {0: 0.0, 1: 0, 2: INF}[semiring]
+    op = {0: np.add, 1: np.bitwise_or, 2: np.minimum}[semiring]
+    dt = np.float64 if semiring == 0 else np.int64
+    Xs = X if semiring == 0 else (X != 0).astype(np.int64) if semiring == 1 else np.minimum(X, INF).astype(np.int64)
+    down = np.full((n, B), zero, dtype=dt)
+    tdown = np.full((s["n_terms"], B), zero, dtype=dt)
+    want_split = []
+    for k in list(range(D, 0, -1)) + [D + 1]:
+        a, b = int(lo[k - 1]), int(lo[k])
+        t = tgt[a:b]
+        assert np.all(np.diff(t) >= 0), "targets ascending within a level"
+        starts = np.flatnonzero(np.r_[True, t[1:] != t[:-1]])
+        ends = np.r_[starts[1:], len(t)] - 1
+        for s0, s1 in zip(starts, ends):
+            if s0 // chunk != s1 // chunk:
+                want_split.append(int(t[s0]) if k <= D else n + int(t[s0]))
+        out = tdown if k == D + 1 else down
+        for e in range(a, b):
+            sv = int(src[e])
+            if sv >= n:
+                v = Xs[sv - n]
+            else:
+                pp = sv if sv >= 0 else ~sv
+                v = down[pp]
+                if semiring == 0 and len(op_c) and sv >= 0:
+                    v = v * op_c[pp]
+            out[tgt[e]] = op(out[tgt[e]], v)
+    assert sorted(want_split) == sorted(int(x) for x in split)
+    Y = np.full((s["cols"], B), zero, dtype=dt)
+    for c in range(s["cols"]):
+        for q in tq[to[c]:to[c + 1]]:
+            d = tdown[q]
+            v = V[tv[q - 1]]
+            if semiring == 0:
+                l = v * d
+            elif semiring == 1:
+                l = d if v != 0 else np.zeros(B, dtype=dt)
+            else:
+                l = np.where((int(v) >= INF) | (d >= INF), INF, int(v) + d)
+            Y[c] = op(Y[c], l)
+    return Y

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import gmr
-from helpers import INF, SEMIRINGS, brute_left, golden_cases, golden_meta, load_case
+from helpers import INF, SEMIRINGS, brute_left, golden_cases, golden_meta, interp_left, load_case
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -324,6 +324,54 @@ def test_left_product(case, sr, B):
     torch.cuda.synchronize()
     Y = engine_outputs(sr, dY.cpu().numpy().view({0: np.float32, 1: np.uint32, 2: np.int32}[sr]), B)
     check(sr, Y, ref)
+
+
+@pytest.fixture(scope="module")
+def mosaic_mid():
+    m = gmr.gen_mosaic(3000, 700, 16, 0.01, 1e-3, 5)
+    g = gmr.repair(m)
+    plan = gmr.Plan.build(g, 3000, 700)
+    eng = gmr.Engine(plan)
+    eng.enable_left(plan)
+    codes = O.expand(g.alpha, g.rules(), g.C())
+    return dict(g=g, plan=plan, eng=eng, codes=codes)
+
+
+@pytest.mark.parametrize("sr", range(3))
+@pytest.mark.parametrize("B", [1, 32, 40])
+def test_left_product_straddling_targets(mosaic_mid, sr, B):
+    """3,000 x 700 mosaic: symbols with many parents / rows are folded by
+    several lane groups (atomic parts into a zeroed value)."""
+    torch = pytest.importorskip("torch")
+    c = mosaic_mid
+    assert len(c["plan"].array("le_split")) > 100
+    X = random_X(sr, 3000, B, 70 + B)
+    ref = brute_left(c["codes"], c["g"].values().astype(np.float32), X, 3000, 700, sr)
+    Xw = engine_inputs(sr, X)
+    dX = torch.from_numpy(Xw.view(np.int32)).cuda()
+    dY = torch.zeros((700, Xw.shape[1]), dtype=torch.int32, device="cuda")
+    for _ in range(2):
+        c["eng"].multiply_left_device(sr, dX.data_ptr(), dY.data_ptr(), B)
+    torch.cuda.synchronize()
+    Y = engine_outputs(sr, dY.cpu().numpy().view({0: np.float32, 1: np.uint32, 2: np.int32}[sr]), B)
+    check(sr, Y, ref)
+
+
+def test_left_product_runlength():
+    """Run-length coefficient on the left child: compared with the FP64
+    evaluation of the plan's transpose arrays."""
+    torch = pytest.importorskip("torch")
+    g = gmr.Grammar.from_arrays(5, [[1, 2], [3, 5], [6, 0], [7, 5]], [8, 0, 6, 0], [1.5, 2.5], kinds=[0, 0, 1, 0],
+                                reps=[1, 1, 3, 1])
+    plan = gmr.Plan.build(g, 2, 3)
+    eng = gmr.Engine(plan)
+    eng.enable_left(plan)
+    X = np.array([[2.0, 0.5], [-1.0, 3.0]], np.float32)
+    dX = torch.from_numpy(X).cuda()
+    dY = torch.zeros((3, 2), dtype=torch.float32, device="cuda")
+    eng.multiply_left_device(0, dX.data_ptr(), dY.data_ptr(), 2)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(dY.cpu().numpy(), interp_left(plan, 0, X), rtol=1e-6)
 
 
 def test_unittest_grammar_runlength():

@@ -3,7 +3,7 @@ import numpy as np
 import pytest
 
 import gmr
-from helpers import INF, SEMIRINGS, brute_left, golden_cases, interp_left, interp_plan, load_case
+from helpers import INF, SEMIRINGS, brute_left, golden_cases, interp_left, interp_left_edges, interp_plan, load_case
 from oracle import oracle as O
 
 
@@ -277,8 +277,37 @@ def test_left_product_structures(case, sr):
         X[rng.random(X.shape) < 0.3] = 1e9
     codes = O.expand(g.alpha, g.rules(), g.C())
     ref = brute_left(codes, case["V"].astype(np.float32), X, rows, cols, sr)
-    Y = interp_left(p, sr, X)
+    for Y in (interp_left(p, sr, X), interp_left_edges(p, sr, X)):
+        if sr == 0:
+            np.testing.assert_allclose(Y, ref, rtol=1e-6, atol=1e-6)
+        else:
+            np.testing.assert_array_equal(Y, ref)
+
+
+@pytest.mark.parametrize("sr", range(3))
+def test_left_edge_lists_straddling_chunks(sr):
+    """A mosaic grammar whose popular symbols have far more than one chunk of
+    edges: the flat edge lists still give x^T M, and le_split is exact."""
+    m = gmr.gen_mosaic(400, 120, 6, 0.02, 1e-3, 4)
+    g = gmr.repair(m)
+    p = gmr.Plan.build(g, 400, 120)
+    p.prepare_left()
+    assert len(p.array("le_split")) > 10
+    rng = np.random.default_rng(sr)
+    X = rng.uniform(-1, 1, (400, 2)) if sr == 0 else (rng.random((400, 2)) < 0.3).astype(np.float64) \
+        if sr == 1 else rng.integers(0, 1000, (400, 2)).astype(np.float64)
+    ref = brute_left(O.expand(g.alpha, g.rules(), g.C()), g.values().astype(np.float32), X, 400, 120, sr)
+    Y = interp_left_edges(p, sr, X)
     if sr == 0:
         np.testing.assert_allclose(Y, ref, rtol=1e-6, atol=1e-6)
     else:
         np.testing.assert_array_equal(Y, ref)
+
+
+def test_left_edge_lists_runlength():
+    g = gmr.Grammar.from_arrays(5, [[1, 2], [3, 5], [6, 0], [7, 5]], [8, 0], [1.5, 2.5], kinds=[0, 0, 1, 0],
+                                reps=[1, 1, 3, 1])
+    p = gmr.Plan.build(g, 2, 3)
+    p.prepare_left()
+    X = np.array([[2.0], [-1.0]])
+    np.testing.assert_allclose(interp_left_edges(p, 0, X), interp_left(p, 0, X), atol=1e-12)
