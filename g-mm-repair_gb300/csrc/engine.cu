@@ -576,9 +576,10 @@ struct Launch {
 struct GraphEntry {
     cudaGraphExec_t exec = nullptr;
     Launch lc{};
-    int64_t launches = 0;  // kernel launches inside the graph
+    int64_t launches = 0;  // kernel launches inside the graph (one iteration for a fixpoint loop)
     const void* X = nullptr;
     void* Y = nullptr;
+    bool fixpoint = false;  // a whole fixpoint loop (conditional while node) rather than one multiply
 };
 
 }  // namespace gmr
@@ -968,7 +969,7 @@ static void multiply_device(gmr_engine* e, int semiring, const void* X, void* Y,
     if (lc.variant == GMR_VARIANT_GRAPH) {
         GraphEntry* hit = nullptr;
         for (auto& g : e->graphs)
-            if (g.exec && g.lc == lc && g.X == X && g.Y == Y) hit = &g;
+            if (g.exec && !g.fixpoint && g.lc == lc && g.X == X && g.Y == Y) hit = &g;
         if (!hit) {
             if (e->graphs.size() >= 8) {
                 cudaGraphExecDestroy(e->graphs.front().exec);
@@ -1582,6 +1583,83 @@ __global__ void k_merge_changed(typename S::T* __restrict__ X, const typename S:
 
 }  // namespace gmr
 
+namespace gmr {
+
+// End of one fixpoint iteration, on one thread: counts it, keeps the loop
+// going while the merge changed something and the count is below the limit,
+// and clears the change flag for the next iteration.
+__global__ void k_fix_step(int* flag, int* count, const int* max_iters, cudaGraphConditionalHandle h) {
+    const int c = *count + 1;
+    *count = c;
+    const int changed = *flag;
+    *flag = 0;
+    cudaGraphSetConditional(h, (changed != 0 && c < *max_iters) ? 1u : 0u);
+}
+
+__global__ void k_set_i32(int* p, int v) { *p = v; }
+
+// The whole loop as one graph: a conditional while node whose body is one
+// multiply (the per-launch kernels, no nested graph), the merge kernel and
+// k_fix_step.  The host launches it once and reads the iteration count.
+static GraphEntry* fixpoint_graph(gmr_engine* e, const Launch& lc, int semiring, void* X, void* Y, int64_t n,
+                                  int* flag, int* count, const int* max_iters) {
+    for (auto& g : e->graphs)
+        if (g.exec && g.fixpoint && g.lc == lc && g.X == X && g.Y == Y) return &g;
+    if (e->graphs.size() >= 8) {
+        cudaGraphExecDestroy(e->graphs.front().exec);
+        e->graphs.erase(e->graphs.begin());
+    }
+    cudaGraph_t graph = nullptr;
+    GMR_CUDA(cudaGraphCreate(&graph, 0));
+    GraphEntry ge;
+    ge.lc = lc;
+    ge.X = X;
+    ge.Y = Y;
+    ge.fixpoint = true;
+    try {
+        cudaGraphConditionalHandle h;
+        GMR_CUDA(cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams cp{};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node;
+        GMR_CUDA(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        GMR_CUDA(cudaStreamBeginCaptureToGraph(e->own_stream, body, nullptr, nullptr, 0,
+                                               cudaStreamCaptureModeThreadLocal));
+        int64_t launches = 0;
+        cudaGraph_t captured = nullptr;
+        try {
+            launch_chain(e, lc, X, Y, e->own_stream, launches);
+            const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)e->sm_count * 8));
+            if (semiring == GMR_BOOLEAN)
+                k_merge_changed<SBool><<<blocks, 256, 0, e->own_stream>>>(static_cast<uint32_t*>(X),
+                                                                         static_cast<const uint32_t*>(Y), n, flag);
+            else
+                k_merge_changed<STrop><<<blocks, 256, 0, e->own_stream>>>(static_cast<int32_t*>(X),
+                                                                         static_cast<const int32_t*>(Y), n, flag);
+            k_fix_step<<<1, 1, 0, e->own_stream>>>(flag, count, max_iters, h);
+            GMR_CUDA(cudaGetLastError());
+        } catch (...) {
+            cudaStreamEndCapture(e->own_stream, &captured);
+            throw;
+        }
+        GMR_CUDA(cudaStreamEndCapture(e->own_stream, &captured));
+        ge.launches = launches + 2;
+        GMR_CUDA(cudaGraphInstantiate(&ge.exec, graph, 0));
+    } catch (...) {
+        cudaGraphDestroy(graph);
+        throw;
+    }
+    cudaGraphDestroy(graph);
+    e->graphs.push_back(ge);
+    return &e->graphs.back();
+}
+
+}  // namespace gmr
+
 extern "C" int gmr_engine_fixpoint(gmr_engine* e, int semiring, void* dX, void* dY, int B, int max_iters,
                                    void* stream, int* iters) {
     return guarded([&] {
@@ -1590,32 +1668,29 @@ extern "C" int gmr_engine_fixpoint(gmr_engine* e, int semiring, void* dX, void* 
             throw Error(GMR_ERR_ARG, "fixpoint needs an idempotent semiring (boolean or tropical)");
         if (e->rows != e->cols) throw Error(GMR_ERR_ARG, "fixpoint needs a square matrix");
         if (B < 1 || max_iters < 0) throw Error(GMR_ERR_ARG, "bad B or max_iters");
+        if (((uintptr_t)dX | (uintptr_t)dY) % 4 != 0) throw Error(GMR_ERR_ARG, "X and Y must be 4-byte aligned");
         std::lock_guard<std::mutex> lk(e->mu);
         DeviceGuard dg(e->device);
         cudaStream_t st = static_cast<cudaStream_t>(stream);
-        const int64_t n = (int64_t)e->rows * words_per_slot(semiring, B);
-        e->sync.ensure(16);
+        if (iters) *iters = 0;
+        if (max_iters == 0) return;
+        Launch lc = resolve_launch(e, semiring, B, dX, dY, nullptr);
+        if (lc.variant == GMR_VARIANT_GRAPH || lc.variant == GMR_VARIANT_PERSISTENT) lc.variant = GMR_VARIANT_FUSED;
+        ensure_scratch(e, lc.Bw);
+        const int64_t n = (int64_t)e->rows * lc.Bw;
+        e->sync.ensure(64);
         int* flag = reinterpret_cast<int*>(static_cast<unsigned char*>(e->sync.p) + 8);
-        int it = 0;
-        for (; it < max_iters; ++it) {
-            multiply_device(e, semiring, dX, dY, B, nullptr, st);
-            GMR_CUDA(cudaMemsetAsync(flag, 0, 4, st));
-            const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)e->sm_count * 8));
-            if (semiring == GMR_BOOLEAN)
-                k_merge_changed<SBool><<<blocks, 256, 0, st>>>(static_cast<uint32_t*>(dX),
-                                                              static_cast<const uint32_t*>(dY), n, flag);
-            else
-                k_merge_changed<STrop><<<blocks, 256, 0, st>>>(static_cast<int32_t*>(dX),
-                                                              static_cast<const int32_t*>(dY), n, flag);
-            GMR_CUDA(cudaGetLastError());
-            GMR_CUDA(cudaMemcpyAsync(e->status_host + 2, flag, 4, cudaMemcpyDeviceToHost, st));
-            GMR_CUDA(cudaStreamSynchronize(st));
-            if (e->status_host[2] == 0) {
-                ++it;
-                break;
-            }
-        }
-        if (iters) *iters = it;
+        int* count = flag + 1;
+        int* limit = flag + 2;
+        GraphEntry* g = fixpoint_graph(e, lc, semiring, dX, dY, n, flag, count, limit);
+        GMR_CUDA(cudaMemsetAsync(flag, 0, 8, st));
+        k_set_i32<<<1, 1, 0, st>>>(limit, max_iters);
+        GMR_CUDA(cudaGetLastError());
+        GMR_CUDA(cudaGraphLaunch(g->exec, st));
+        GMR_CUDA(cudaMemcpyAsync(e->status_host + 2, count, 4, cudaMemcpyDeviceToHost, st));
+        GMR_CUDA(cudaStreamSynchronize(st));
+        if (iters) *iters = e->status_host[2];
+        e->last_launches = g->launches * e->status_host[2] + 1;
     });
 }
 

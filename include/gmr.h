@@ -356,8 +356,10 @@ int gmr_engine_multiply_left(gmr_engine* e, int semiring, const void* dX, void* 
  * the set of nodes that reach it (x | Mx, repeated); GMR_TROPICAL relaxes
  * distances to the initial set (min(x, Mx), Bellman-Ford).  dX holds the start
  * and receives the fixpoint; dY is scratch of the same shape.  Each iteration
- * is one (graph-replayed) multiply and one merge kernel that flags changes;
- * stops when an iteration changes nothing (it is counted) or after max_iters.
+ * is one multiply and one merge kernel that flags changes; stops when an
+ * iteration changes nothing (it is counted) or after max_iters.  The whole
+ * loop is one CUDA graph launch (a conditional while node decides on the
+ * device whether to run the next iteration), cached per (X, Y, B).
  * *iters = iterations run.  Synchronous on `stream`.  No counterpart function
  * in the reference, whose semiring sweeps are the single steps of these
  * iterations. */

@@ -305,6 +305,45 @@ def test_fixpoint_reachability_and_distances(name, sr):
     check(sr, out, ref)
 
 
+@pytest.mark.parametrize("sr", [1, 2])
+def test_fixpoint_iteration_limit_and_repeat(sr):
+    """max_iters caps the device-side loop (0 runs nothing, 1 runs one merge);
+    a second call on the same buffers replays the cached loop graph."""
+    torch = pytest.importorskip("torch")
+    c = load_case("graph_400" if sr == 1 else "graph_w300")
+    n = int(c["rows"])
+    g = gmr.Grammar.from_arrays(int(c["alpha"]), c["rules"], c["C"], c["V"])
+    eng = gmr.Engine(gmr.Plan.build(g, n, n))
+    sched = O.RefSchedule(int(c["alpha"]), c["rules"], c["C"])
+    rng = np.random.default_rng(5)
+    B = 32 if sr == 1 else 2
+    if sr == 1:
+        X = (rng.random((n, B)) < 0.01).astype(np.float32)
+    else:
+        X = np.full((n, B), 1e9, dtype=np.float32)
+        X[rng.random((n, B)) < 0.01] = 0.0
+    Xw = engine_inputs(sr, X) if sr == 1 else X.astype(np.int32)
+    dX = torch.from_numpy(Xw.view(np.int32).copy()).cuda()
+    dY = torch.empty_like(dX)
+    assert eng.fixpoint_device(sr, dX.data_ptr(), dY.data_ptr(), B, max_iters=0) == 0
+    np.testing.assert_array_equal(dX.cpu().numpy(), Xw.view(np.int32))
+    assert eng.fixpoint_device(sr, dX.data_ptr(), dY.data_ptr(), B, max_iters=1) == 1
+    Y = oracle_columns(sched, sr, c["V"], X, n, n)
+    one = np.maximum(X, Y) if sr == 1 else np.minimum(X, Y)
+    out = engine_outputs(sr, dX.cpu().numpy().view(np.uint32 if sr == 1 else np.int32), B)
+    check(sr, out, one)
+    total = 1
+    for _ in range(200):
+        it = eng.fixpoint_device(sr, dX.data_ptr(), dY.data_ptr(), B, max_iters=2)
+        total += it
+        if it < 2:
+            break
+    full = engine_outputs(sr, dX.cpu().numpy().view(np.uint32 if sr == 1 else np.int32), B)
+    assert eng.fixpoint_device(sr, dX.data_ptr(), dY.data_ptr(), B) == 1  # at the fixpoint: one idle iteration
+    np.testing.assert_array_equal(engine_outputs(sr, dX.cpu().numpy().view(np.uint32 if sr == 1 else np.int32), B),
+                                  full)
+
+
 @pytest.mark.parametrize("sr", range(3))
 @pytest.mark.parametrize("B", [1, 8, 33])
 def test_left_product(case, sr, B):
