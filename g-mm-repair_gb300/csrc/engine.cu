@@ -592,6 +592,9 @@ struct gmr_engine {
     std::vector<int64_t> lvl_off, em_off, seg_off;
     gmr::DevBuf ops, op_c, em_src, em_row, seg_row, seg_start, term_val, term_col, V;
     gmr::DevBuf arena, T, hX, hY;  // scratch
+    gmr::DevBuf hX2, hY2;          // second staging pair of the pipelined host-buffer multiply
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;
+    cudaEvent_t pipe_ev[6] = {};    // per staging slot: X copied in, multiply done, Y copied out
     gmr::DevBuf d_lvl_off, d_em_off, d_seg_off, sync;  // persistent variant: level tables, barrier + error words
     // The emissions again, ordered by (source chunk, row, source) within each
     // level, with row segments per chunk: chunk c of level k covers source
@@ -1180,6 +1183,53 @@ extern "C" int gmr_engine_multiply_host(gmr_engine* e, int semiring, const void*
     });
 }
 
+extern "C" int gmr_engine_multiply_host_many(gmr_engine* e, int semiring, const void* const* hX, void* const* hY,
+                                             int n, int B, const gmr_config* cfg) {
+    return guarded([&] {
+        if (!e || (n > 0 && (!hX || !hY))) throw Error(GMR_ERR_ARG, "null argument");
+        if (B < 1 || n < 0) throw Error(GMR_ERR_ARG, "bad B or n");
+        for (int i = 0; i < n; ++i)
+            if ((!hX[i] && e->cols > 0) || (!hY[i] && e->rows > 0)) throw Error(GMR_ERR_ARG, "null X or Y");
+        std::lock_guard<std::mutex> lk(e->mu);
+        DeviceGuard dg(e->device);
+        const size_t xb = (size_t)e->cols * words_per_slot(semiring, B) * 4;
+        const size_t yb = (size_t)e->rows * words_per_slot(semiring, B) * 4;
+        e->hX.ensure(xb);
+        e->hY.ensure(yb);
+        e->hX2.ensure(xb);
+        e->hY2.ensure(yb);
+        if (!e->copy_in) GMR_CUDA(cudaStreamCreateWithFlags(&e->copy_in, cudaStreamNonBlocking));
+        if (!e->copy_out) GMR_CUDA(cudaStreamCreateWithFlags(&e->copy_out, cudaStreamNonBlocking));
+        for (auto& ev : e->pipe_ev)
+            if (!ev) GMR_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        void* dx[2] = {e->hX.p, e->hX2.p};
+        void* dy[2] = {e->hY.p, e->hY2.p};
+        cudaStream_t st = e->own_stream;
+        // multiply i runs in staging slot i % 2: its X copy overlaps multiply
+        // i - 1, its Y copy overlaps multiply i + 1
+        for (int i = 0; i < n; ++i) {
+            const int k = i & 1;
+            cudaEvent_t x_in = e->pipe_ev[3 * k], done = e->pipe_ev[3 * k + 1], y_out = e->pipe_ev[3 * k + 2];
+            if (i >= 2) GMR_CUDA(cudaStreamWaitEvent(e->copy_in, done, 0));
+            if (xb) GMR_CUDA(cudaMemcpyAsync(dx[k], hX[i], xb, cudaMemcpyHostToDevice, e->copy_in));
+            GMR_CUDA(cudaEventRecord(x_in, e->copy_in));
+            GMR_CUDA(cudaStreamWaitEvent(st, x_in, 0));
+            if (i >= 2) GMR_CUDA(cudaStreamWaitEvent(st, y_out, 0));
+            e->last_persistent = false;
+            multiply_device(e, semiring, dx[k], dy[k], B, cfg, st);
+            GMR_CUDA(cudaEventRecord(done, st));
+            GMR_CUDA(cudaStreamWaitEvent(e->copy_out, done, 0));
+            if (yb) GMR_CUDA(cudaMemcpyAsync(hY[i], dy[k], yb, cudaMemcpyDeviceToHost, e->copy_out));
+            GMR_CUDA(cudaEventRecord(y_out, e->copy_out));
+        }
+        GMR_CUDA(cudaStreamSynchronize(e->copy_out));
+        GMR_CUDA(cudaStreamSynchronize(st));
+        if (e->last_persistent && e->status_host[0] != 0)
+            throw Error(GMR_ERR_TIMEOUT, "persistent sweep: a grid-barrier wait gave up at phase " +
+                                             std::to_string(e->status_host[1]) + "; Y is not valid");
+    });
+}
+
 extern "C" int gmr_engine_time_launches(gmr_engine* e, int semiring, const void* dX, void* dY, int B,
                                         const gmr_config* cfg, void* stream, float* ms, int cap, int* n) {
     return guarded([&] {
@@ -1308,7 +1358,11 @@ extern "C" void gmr_engine_free(gmr_engine* e) {
         for (auto& g : e->graphs)
             if (g.exec) cudaGraphExecDestroy(g.exec);
         for (auto* b : e->schedule_bufs()) b->release();
-        for (auto* b : {&e->arena, &e->T, &e->hX, &e->hY}) b->release();
+        for (auto* b : {&e->arena, &e->T, &e->hX, &e->hY, &e->hX2, &e->hY2}) b->release();
+        for (auto ev : e->pipe_ev)
+            if (ev) cudaEventDestroy(ev);
+        for (auto s2 : {e->copy_in, e->copy_out})
+            if (s2) cudaStreamDestroy(s2);
         if (e->own_stream) cudaStreamDestroy(e->own_stream);
         if (e->status_host) cudaFreeHost(e->status_host);
         if (prev >= 0) cudaSetDevice(prev);

@@ -461,6 +461,18 @@ class Engine:
         """Upload the reverse adjacency needed by the left product y = x^T M."""
         _check(lib().gmr_engine_enable_left(self._h, plan._h))
 
+    def multiply_host_many(self, semiring, x_ptrs, y_ptrs, B: int, **cfg):
+        """n multiplies from host X buffers into host Y buffers (raw addresses,
+        page-locked for the copies to overlap), pipelined through two device
+        staging pairs."""
+        n = len(x_ptrs)
+        if len(y_ptrs) != n:
+            raise ValueError("as many Y buffers as X buffers")
+        xs = (C.c_void_p * n)(*[C.c_void_p(int(p)) for p in x_ptrs])
+        ys = (C.c_void_p * n)(*[C.c_void_p(int(p)) for p in y_ptrs])
+        c = self._cfg(**cfg)
+        _check(lib().gmr_engine_multiply_host_many(self._h, semiring_id(semiring), xs, ys, n, B, C.byref(c)))
+
     def multiply_left_device(self, semiring, x_ptr: int, y_ptr: int, B: int, stream: int = 0):
         """y[cols][words] = x^T M for x[rows][words] (device pointers)."""
         _check(lib().gmr_engine_multiply_left(self._h, semiring_id(semiring), C.c_void_p(x_ptr),

@@ -109,6 +109,8 @@ _SIGS = {
     "gmr_engine_create": (C.c_int, [P, C.c_int, C.POINTER(P)]),
     "gmr_engine_multiply": (C.c_int, [P, C.c_int, P, P, C.c_int, C.POINTER(Config), P]),
     "gmr_engine_multiply_host": (C.c_int, [P, C.c_int, P, P, C.c_int, C.POINTER(Config)]),
+    "gmr_engine_multiply_host_many": (C.c_int, [P, C.c_int, C.POINTER(P), C.POINTER(P), C.c_int, C.c_int,
+                                                C.POINTER(Config)]),
     "gmr_engine_time_launches": (C.c_int, [P, C.c_int, P, P, C.c_int, C.POINTER(Config), P, F32P, C.c_int,
                                            C.POINTER(C.c_int)]),
     "gmr_engine_set_level_variants": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(C.c_uint8), C.c_int]),

@@ -256,6 +256,13 @@ int gmr_engine_multiply(gmr_engine* e, int semiring, const void* dX, void* dY,
 /* Host buffers: copies X in, multiplies, copies Y out, synchronous. */
 int gmr_engine_multiply_host(gmr_engine* e, int semiring, const void* hX,
                              void* hY, int B, const gmr_config* cfg);
+/* n independent multiplies with host buffers (hX[i] -> hY[i]), pipelined:
+ * two device staging pairs, so that copying X of multiply i+1 in and Y of
+ * multiply i-1 out overlap multiply i.  The copies overlap only when the host
+ * buffers are page-locked (cudaHostAlloc / cudaHostRegister).  Synchronous:
+ * returns when every hY[i] is written. */
+int gmr_engine_multiply_host_many(gmr_engine* e, int semiring, const void* const* hX,
+                                  void* const* hY, int n, int B, const gmr_config* cfg);
 /* Runs one multiply launch by launch (no graph) with a CUDA event pair
  * around every launch and writes the device time of each launch (ms) to
  * ms[0..*n): launch 0 is the prologue (Y = zero, terminal values), launch k

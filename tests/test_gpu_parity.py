@@ -305,6 +305,26 @@ def test_fixpoint_reachability_and_distances(name, sr):
     check(sr, out, ref)
 
 
+@pytest.mark.parametrize("sr", range(3))
+@pytest.mark.parametrize("n", [0, 1, 5])
+def test_pipelined_host_multiplies(case, sr, n):
+    """gmr_engine_multiply_host_many: every hY[i] equals its own multiply."""
+    torch = pytest.importorskip("torch")
+    rows, cols, B = int(case["rows"]), int(case["cols"]), 33
+    eng = gmr.Engine(case["plan"])
+    Xs = [engine_inputs(sr, random_X(sr, cols, B, 300 + i)) for i in range(n)]
+    Xp = [torch.from_numpy(x.view(np.int32)).pin_memory() for x in Xs]
+    Yp = [torch.zeros((rows, x.shape[1]), dtype=torch.int32).pin_memory() for x in Xs]
+    eng.multiply_host_many(sr, [x.data_ptr() for x in Xp], [y.data_ptr() for y in Yp], B)
+    for i in range(n):
+        want = eng.multiply(Xs[i], sr, B=B)
+        got = Yp[i].numpy().view(want.dtype)
+        if sr == 0:
+            assert np.max(np.abs(got - want)) <= 1e-5 * max(1.0, float(np.max(np.abs(want))))
+        else:
+            np.testing.assert_array_equal(got, want)
+
+
 @pytest.mark.parametrize("sr", [1, 2])
 def test_fixpoint_iteration_limit_and_repeat(sr):
     """max_iters caps the device-side loop (0 runs nothing, 1 runs one merge);
