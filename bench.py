@@ -618,6 +618,7 @@ def main():
     vbytes = 4.0 * words * (st["n_emit"] + st["n_term_emit"] + 3 * st["n_ops"])
     ceil_l2 = gmr.measure_gather_bandwidth(64 << 20, device=local)
     ceil_hbm = gmr.measure_gather_bandwidth(4 << 30, device=local)
+    l2_seq = gmr.measure_gather_bandwidth(64 << 20, device=local, sequential=True)
     value_gbs = vbytes / (level_ms / 1000.0) / 1e9
     step_gbs = alg_total / (ms_per_step / 1000.0) / 1e9
     traffic = None
@@ -676,6 +677,7 @@ def main():
                      "step_alg_gbs": step_gbs,
                      "gather_ceiling": {"value_bytes_per_multiply": vbytes, "achieved_gbs": value_gbs,
                                         "l2_random_128B_gbs": ceil_l2, "hbm_random_128B_gbs": ceil_hbm,
+                                        "l2_sequential_gbs": l2_seq,
                                         "frac_of_l2_ceiling": value_gbs / ceil_l2}},
         "e2e": {"value": e2e_value, "unit": "vectors/s", "h2d_bytes_per_step": int(cols * words * 4),
                 "d2h_bytes_per_step": int(rows * words * 4), "api": "gmr_engine_multiply_host_many (pipelined)",

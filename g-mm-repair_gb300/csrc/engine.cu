@@ -1866,7 +1866,8 @@ extern "C" void gmr_pack_free(gmr_pack* p) {
 // addresses; its ceiling is the random-line gather bandwidth of the GPU, from
 // L2 (working set that fits) and from HBM (one that does not).  This
 // calibration measures both with the same access pattern (indices taken
-// modulo the buffer's line count, so every access is in bounds).
+// modulo the buffer's line count, so every access is in bounds); the
+// sequential mode reads the same lines in order, for the plain read bandwidth.
 namespace gmr {
 
 __device__ __forceinline__ unsigned mix32(unsigned x) {
@@ -1879,7 +1880,7 @@ __device__ __forceinline__ unsigned mix32(unsigned x) {
 }
 
 __global__ void __launch_bounds__(256) k_gather_lines(const float4* __restrict__ buf, unsigned nlines, int64_t items,
-                                                      float* __restrict__ sink) {
+                                                      bool sequential, float* __restrict__ sink) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
     float acc = 0.0f;
     for (int64_t i = t; i < items * 8; i += 4 * stride) {
@@ -1887,7 +1888,8 @@ __global__ void __launch_bounds__(256) k_gather_lines(const float4* __restrict__
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int64_t ii = i + j * stride;
-            const unsigned line = mix32((unsigned)(ii >> 3)) % nlines;
+            const unsigned li = (unsigned)(ii >> 3);
+            const unsigned line = (sequential ? li : mix32(li)) % nlines;
             v[j] = ii < items * 8 ? __ldg(buf + (int64_t)line * 8 + (ii & 7)) : make_float4(0.f, 0.f, 0.f, 0.f);
         }
 #pragma unroll
@@ -1898,7 +1900,7 @@ __global__ void __launch_bounds__(256) k_gather_lines(const float4* __restrict__
 
 }  // namespace gmr
 
-extern "C" int gmr_measure_gather_bandwidth(int device, int64_t buffer_bytes, float* gbs) {
+extern "C" int gmr_measure_gather_bandwidth(int device, int64_t buffer_bytes, int sequential, float* gbs) {
     return guarded([&] {
         if (!gbs || buffer_bytes < 4096 || buffer_bytes > (int64_t)64 << 30) throw Error(GMR_ERR_ARG, "bad argument");
         DeviceGuard dg(device);
@@ -1914,12 +1916,12 @@ extern "C" int gmr_measure_gather_bandwidth(int device, int64_t buffer_bytes, fl
         GMR_CUDA(cudaEventCreate(&a));
         GMR_CUDA(cudaEventCreate(&b));
         k_gather_lines<<<sms * 16, 256>>>(static_cast<const float4*>(buf.p), (unsigned)lines, items / 10,
-                                          static_cast<float*>(sink.p));
+                                          sequential != 0, static_cast<float*>(sink.p));
         float best = 0.0f;
         for (int r = 0; r < 3; ++r) {
             cudaEventRecord(a);
             k_gather_lines<<<sms * 16, 256>>>(static_cast<const float4*>(buf.p), (unsigned)lines, items,
-                                              static_cast<float*>(sink.p));
+                                              sequential != 0, static_cast<float*>(sink.p));
             cudaEventRecord(b);
             GMR_CUDA(cudaEventSynchronize(b));
             float ms = 0.0f;

@@ -550,10 +550,11 @@ class Pack:
         self.close()
 
 
-def measure_gather_bandwidth(buffer_bytes: int, device: int = 0) -> float:
-    """Random 128-byte line gather bandwidth (GB/s) over a buffer of that size."""
+def measure_gather_bandwidth(buffer_bytes: int, device: int = 0, sequential: bool = False) -> float:
+    """Random (or, sequential=True, in-order) 128-byte line read bandwidth
+    (GB/s) over a buffer of that size."""
     g = C.c_float()
-    _check(lib().gmr_measure_gather_bandwidth(device, int(buffer_bytes), C.byref(g)))
+    _check(lib().gmr_measure_gather_bandwidth(device, int(buffer_bytes), int(bool(sequential)), C.byref(g)))
     return float(g.value)
 
 

@@ -336,8 +336,9 @@ int gmr_engine_choose_learned(gmr_engine* e, const gmr_plan* p, const gmr_mlp* m
 /* Random 128-byte line gather bandwidth (GB/s) of the device over a buffer
  * of buffer_bytes: the access pattern of the sweep's value gathers.  A
  * buffer that fits in L2 gives the L2 ceiling, a large one the HBM ceiling.
+ * sequential != 0 reads the lines in order instead (plain read bandwidth).
  * Allocates the buffer for the measurement. */
-int gmr_measure_gather_bandwidth(int device, int64_t buffer_bytes, float* gbs);
+int gmr_measure_gather_bandwidth(int device, int64_t buffer_bytes, int sequential, float* gbs);
 
 /* Status of the engine's last GMR_VARIANT_PERSISTENT multiply, valid once the
  * stream it ran on has been synchronized: *failed != 0 when a grid-barrier
