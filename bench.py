@@ -85,6 +85,23 @@ def cached_grammar(key: str, make):
     return g, info | {"cached": False}
 
 
+REPAIR_ON_GPU = True  # the reference arm builds its grammar with the host compressor
+
+
+def repair_device():
+    """GPU of this rank for the RePair compressor (identical grammar to the
+    host compressor), or None for the host compressor."""
+    if not REPAIR_ON_GPU:
+        return None
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return int(os.environ.get("LOCAL_RANK", "0"))
+    except ImportError:
+        pass
+    return None
+
+
 def mosaic_grammar(rows, cols, F, sw, mu, seed):
     import gmr
 
@@ -92,10 +109,11 @@ def mosaic_grammar(rows, cols, F, sw, mu, seed):
         t0 = time.perf_counter()
         m = gmr.gen_mosaic(rows, cols, F, sw, mu, seed)
         t1 = time.perf_counter()
-        g = gmr.repair(m)
+        g = gmr.repair(m, device=repair_device())
         t2 = time.perf_counter()
         log(f"grammar mosaic {rows}x{cols}: nnz={m.nnz} gen {t1 - t0:.1f}s repair {t2 - t1:.1f}s")
-        return g, {"nnz": int(m.nnz), "gen_s": round(t1 - t0, 2), "repair_s": round(t2 - t1, 2)}
+        return g, {"nnz": int(m.nnz), "gen_s": round(t1 - t0, 2), "repair_s": round(t2 - t1, 2),
+                   "repair_on": "gpu" if repair_device() is not None else "host"}
 
     return cached_grammar(f"mosaic-{rows}x{cols}-f{F}-s{seed}", make)
 
@@ -109,10 +127,11 @@ def graph_grammar(weighted: bool):
         t0 = time.perf_counter()
         m = gmr.gen_copy_graph(nodes, deg, cp, weighted, seed)
         t1 = time.perf_counter()
-        g = gmr.repair(m)
+        g = gmr.repair(m, device=repair_device())
         t2 = time.perf_counter()
         log(f"grammar graph {nodes}: nnz={m.nnz} gen {t1 - t0:.1f}s repair {t2 - t1:.1f}s")
-        return g, {"nnz": int(m.nnz), "gen_s": round(t1 - t0, 2), "repair_s": round(t2 - t1, 2)}
+        return g, {"nnz": int(m.nnz), "gen_s": round(t1 - t0, 2), "repair_s": round(t2 - t1, 2),
+                   "repair_on": "gpu" if repair_device() is not None else "host"}
 
     return cached_grammar(f"graph-{nodes}-d{deg}-w{int(weighted)}-s{seed}", make)
 
@@ -410,6 +429,32 @@ def run_pack8(args):
     return 0
 
 
+def run_repair_compare(args):
+    """RePair of the workload's matrix on the GPU and on all host cores: both
+    timed, grammars compared symbol for symbol."""
+    import gmr
+
+    if args.workload in MOSAICS:
+        r, c, F, sw, mu, seed = MOSAICS[args.workload]
+        m = gmr.gen_mosaic(r, c, F, sw, mu, seed)
+    else:
+        nodes, deg, cp, seed = GRAPH
+        m = gmr.gen_copy_graph(nodes, deg, cp, args.semiring == "tropical", seed)
+    gmr.repair(gmr.gen_mosaic(500, 100, 8, 0.02, 1e-3, 1), device=0)  # loads the kernels
+    t = time.perf_counter()
+    gd = gmr.repair(m, device=0)
+    td = time.perf_counter() - t
+    t = time.perf_counter()
+    gh = gmr.repair(m)
+    th = time.perf_counter() - t
+    same = gd.alpha == gh.alpha and np.array_equal(gd.rules(), gh.rules()) and np.array_equal(gd.C(), gh.C())
+    print(json.dumps({"metric": "RePair seconds", "unit": "s", "value": td, "higher_is_better": False,
+                      "config": {"workload": args.workload, "symbols": int(m.info.len), "nnz": int(m.nnz)},
+                      "host_s": th, "host_threads": os.cpu_count(), "speedup": th / td, "identical": bool(same),
+                      "rules": int(len(gd.rules())), "C": int(len(gd.C()))}))
+    return 0
+
+
 def run_other_op(args):
     """Left product (Y = X^T M) or fixpoint iteration timed on the workload's grammar."""
     import torch
@@ -475,16 +520,21 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--dump-launches", action="store_true", help="per-launch times and level sizes to stderr")
     ap.add_argument("--no-cusparse", action="store_true", help="skip the cuSPARSE CSR baseline")
-    ap.add_argument("--op", choices=["right", "left", "fixpoint"], default="right",
-                    help="right: Y = M X (the headline); left: Y = X^T M; fixpoint: X <- X (+) M X to convergence")
+    ap.add_argument("--op", choices=["right", "left", "fixpoint", "repair"], default="right",
+                    help="right: Y = M X (the headline); left: Y = X^T M; fixpoint: X <- X (+) M X to convergence; "
+                         "repair: RePair of the workload's matrix on the GPU vs the host")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.semiring is None:
         args.semiring = "boolean" if args.workload == "graph-16777216" else "plustimes"
     if args.impl == "reference":
+        global REPAIR_ON_GPU
+        REPAIR_ON_GPU = False
         return run_reference(args)
     if args.workload == "pack8":
         return run_pack8(args)
+    if args.op == "repair":
+        return run_repair_compare(args)
     if args.op != "right":
         return run_other_op(args)
 

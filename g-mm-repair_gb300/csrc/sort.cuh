@@ -1,6 +1,7 @@
-// Device-wide primitives of the schedule builder: exclusive scan of uint32
-// counts and a stable least-significant-digit radix sort of 64-bit keys that
-// optionally carry a 32-bit value.
+// Device-wide primitives of the schedule builder and the RePair compressor:
+// scans of uint32 (exclusive sum, inclusive maximum) and a stable
+// least-significant-digit radix sort of 64-bit keys that optionally carry a
+// 32-bit value.
 //
 // Scan: reduce-then-scan in three launches per level of recursion (tile sums,
 // scan of the tile sums, scan of each tile from its offset).
@@ -26,95 +27,126 @@ constexpr int kTile = kThreads * kItems;
 inline int64_t tiles(int64_t n) { return (n + kTile - 1) / kTile; }
 inline int grid_for(int64_t n) { return (int)std::min<int64_t>(std::max<int64_t>((n + kThreads - 1) / kThreads, 1), 152 * 32); }
 
-// Block-wide exclusive scan of one value per thread (blockDim.x == kThreads).
+struct SumOp {
+    static constexpr uint32_t identity = 0;
+    __device__ __forceinline__ uint32_t operator()(uint32_t a, uint32_t b) const { return a + b; }
+};
+struct MaxOp {
+    static constexpr uint32_t identity = 0;
+    __device__ __forceinline__ uint32_t operator()(uint32_t a, uint32_t b) const { return a > b ? a : b; }
+};
+
+// Block-wide exclusive scan of one value per thread (blockDim.x == kThreads);
+// *total = the block's reduction.
+template <class Op>
 __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
     __shared__ uint32_t warp_sums[kThreads / 32];
+    const Op op;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t x = v;
+    uint32_t x = v;  // inclusive within the warp
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
+        if (lane >= o) x = op(y, x);
     }
+    uint32_t ex = __shfl_up_sync(0xffffffffu, x, 1);  // exclusive within the warp
+    if (lane == 0) ex = Op::identity;
     if (lane == 31) warp_sums[warp] = x;
     __syncthreads();
     if (warp == 0) {
-        uint32_t w = lane < kThreads / 32 ? warp_sums[lane] : 0;
+        uint32_t w = lane < kThreads / 32 ? warp_sums[lane] : Op::identity;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= o) w += y;
+            if (lane >= o) w = op(y, w);
         }
         if (lane < kThreads / 32) warp_sums[lane] = w;
     }
     __syncthreads();
-    const uint32_t base = warp ? warp_sums[warp - 1] : 0;
+    const uint32_t base = warp ? warp_sums[warp - 1] : Op::identity;
     *total = warp_sums[kThreads / 32 - 1];
     __syncthreads();
-    return base + x - v;
+    return op(base, ex);
 }
 
+template <class Op>
 __global__ void __launch_bounds__(kThreads) k_scan_reduce(const uint32_t* __restrict__ in, int64_t n,
                                                           uint32_t* __restrict__ sums) {
+    const Op op;
     const int64_t base = (int64_t)blockIdx.x * kTile;
-    uint32_t s = 0;
+    uint32_t s = Op::identity;
 #pragma unroll
     for (int j = 0; j < kItems; ++j) {
         const int64_t i = base + j * kThreads + threadIdx.x;
-        if (i < n) s += in[i];
+        if (i < n) s = op(s, in[i]);
     }
     uint32_t total;
-    block_exclusive_scan(s, &total);
+    block_exclusive_scan<Op>(s, &total);
     if (threadIdx.x == 0) sums[blockIdx.x] = total;
 }
 
-// out[i] = offs[tile] + sum of in[tile start .. i); out[n] = total (last tile).
-// in and out may be the same array.
+// Exclusive (or inclusive) scan of each tile from its offset offs[tile];
+// out[n] = the whole reduction (exclusive scans only).  in and out may be the
+// same array.
+template <class Op, bool INCLUSIVE>
 __global__ void __launch_bounds__(kThreads) k_scan_down(const uint32_t* in, uint32_t* out, int64_t n,
                                                         const uint32_t* __restrict__ offs) {
+    const Op op;
     const int64_t base = (int64_t)blockIdx.x * kTile + (int64_t)threadIdx.x * kItems;
-    uint32_t v[kItems], s = 0;
+    uint32_t v[kItems], s = Op::identity;
 #pragma unroll
     for (int j = 0; j < kItems; ++j) {
-        v[j] = base + j < n ? in[base + j] : 0;
-        s += v[j];
+        v[j] = base + j < n ? in[base + j] : Op::identity;
+        s = op(s, v[j]);
     }
     uint32_t total;
-    uint32_t run = block_exclusive_scan(s, &total) + (offs ? offs[blockIdx.x] : 0);
+    const uint32_t off = offs ? offs[blockIdx.x] : Op::identity;
+    uint32_t run = op(off, block_exclusive_scan<Op>(s, &total));
 #pragma unroll
     for (int j = 0; j < kItems; ++j) {
+        if (INCLUSIVE) run = op(run, v[j]);
         if (base + j < n) out[base + j] = run;
-        run += v[j];
+        if (!INCLUSIVE) run = op(run, v[j]);
     }
-    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = (offs ? offs[blockIdx.x] : 0) + total;
+    if (!INCLUSIVE && blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = op(off, total);
 }
 
-// uint32 words of scratch exclusive_scan needs for n items.
+// uint32 words of scratch a scan of n items needs.
 inline int64_t scan_scratch(int64_t n) {
     int64_t s = 0;
     for (int64_t m = tiles(n); m > 1; m = tiles(m)) s += m + 1;
     return s + 1;
 }
 
-// Exclusive scan of in[0, n) into out[0, n], out[n] = total; out may alias in
-// and must hold n + 1 words.  tmp holds scan_scratch(n) words.
-inline void exclusive_scan(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* tmp, cudaStream_t st) {
+template <class Op, bool INCLUSIVE>
+inline void scan(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* tmp, cudaStream_t st) {
     if (n <= 0) {
-        GMR_CUDA(cudaMemsetAsync(out, 0, sizeof(uint32_t), st));
+        if (!INCLUSIVE) GMR_CUDA(cudaMemsetAsync(out, 0, sizeof(uint32_t), st));
         return;
     }
     const int64_t nb = tiles(n);
     if (nb == 1) {
-        k_scan_down<<<1, kThreads, 0, st>>>(in, out, n, nullptr);
+        k_scan_down<Op, INCLUSIVE><<<1, kThreads, 0, st>>>(in, out, n, nullptr);
     } else {
-        k_scan_reduce<<<(unsigned)nb, kThreads, 0, st>>>(in, n, tmp);
-        exclusive_scan(tmp, tmp, nb, tmp + nb + 1, st);
-        k_scan_down<<<(unsigned)nb, kThreads, 0, st>>>(in, out, n, tmp);
+        k_scan_reduce<Op><<<(unsigned)nb, kThreads, 0, st>>>(in, n, tmp);
+        scan<Op, false>(tmp, tmp, nb, tmp + nb + 1, st);
+        k_scan_down<Op, INCLUSIVE><<<(unsigned)nb, kThreads, 0, st>>>(in, out, n, tmp);
     }
     GMR_CUDA(cudaGetLastError());
 }
 
-__global__ void __launch_bounds__(kThreads) k_radix_hist(const uint64_t* __restrict__ keys, int64_t n, int shift,
+// Exclusive sum of in[0, n) into out[0, n], out[n] = total; out may alias in
+// and must hold n + 1 words.  tmp holds scan_scratch(n) words.
+inline void exclusive_scan(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* tmp, cudaStream_t st) {
+    scan<SumOp, false>(in, out, n, tmp, st);
+}
+
+// Inclusive running maximum of in[0, n) into out[0, n) (out may alias in).
+inline void inclusive_max_scan(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* tmp, cudaStream_t st) {
+    scan<MaxOp, true>(in, out, n, tmp, st);
+}
+
+static __global__ void __launch_bounds__(kThreads) k_radix_hist(const uint64_t* __restrict__ keys, int64_t n, int shift,
                                                          int64_t nblk, uint32_t* __restrict__ counts) {
     __shared__ uint32_t h[256];
     h[threadIdx.x] = 0;

@@ -247,9 +247,14 @@ class Grammar:
         return cls(h)
 
 
-def repair(m: Csrv, threads=0) -> Grammar:
+def repair(m: Csrv, threads=0, device: int | None = None) -> Grammar:
+    """RePair grammar of a CSRV string on the host (threads), or the identical
+    grammar computed on GPU `device`."""
     h = C.c_void_p()
-    _check(lib().gmr_repair_compress(m._h, threads, C.byref(h)))
+    if device is None:
+        _check(lib().gmr_repair_compress(m._h, threads, C.byref(h)))
+    else:
+        _check(lib().gmr_repair_compress_device(m._h, int(device), C.byref(h)))
     return Grammar(h)
 
 

@@ -95,6 +95,7 @@ _SIGS = {
                                  C.POINTER(P)]),
     "gmr_gen_copy_graph": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_int, C.c_uint64, C.c_int, C.POINTER(P)]),
     "gmr_repair_compress": (C.c_int, [P, C.c_int, C.POINTER(P)]),
+    "gmr_repair_compress_device": (C.c_int, [P, C.c_int, C.POINTER(P)]),
     "gmr_plan_build": (C.c_int, [P, C.c_int, C.c_int, C.POINTER(P)]),
     "gmr_plan_build_device": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(P)]),
     "gmr_plan_from_layered": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(LayeredRule), I32P, I32P,

@@ -24,7 +24,7 @@ LIB = PKG_DIR / "libgmr.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_SOURCES = ["grammar_io.cpp", "generators.cpp", "repair.cpp", "plan.cpp"]
-CUDA_SOURCES = ["engine.cu", "learn.cu", "plan_device.cu"]
+CUDA_SOURCES = ["engine.cu", "learn.cu", "plan_device.cu", "repair_device.cu"]
 
 
 def nvcc_path() -> str:

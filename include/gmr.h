@@ -162,6 +162,11 @@ int gmr_gen_copy_graph(int nodes, int degree, double copy_prob, int weighted,
 /* Grammar compression of a CSRV string by rounds of RePair pair
  * replacement (most frequent pairs first; rules never span a row end). */
 int gmr_repair_compress(const gmr_csrv* m, int n_threads, gmr_grammar** out);
+/* The same grammar as gmr_repair_compress (identical rules and C), computed on
+ * GPU `device`: per round one radix sort of the pair occurrences, one of the
+ * candidates, and scans for the counts and the greedy replacement choices.
+ * Needs about 48 bytes of device memory per input symbol. */
+int gmr_repair_compress_device(const gmr_csrv* m, int device, gmr_grammar** out);
 
 /* ------------------------------------------------------------------ */
 /* Schedule ("plan"): level-major, child-sorted layout                 */
