@@ -44,7 +44,7 @@ __global__ void k_fill_i32(int32_t* a, int64_t n, int32_t v) {
 }
 
 // One relaxation round of the levels; *changed is set when a level rose.
-__global__ void k_level_round(const int2* __restrict__ R, const int32_t* __restrict__ kind, int32_t alpha, int64_t n,
+__global__ void k_relax_levels(const int2* __restrict__ R, const int32_t* __restrict__ kind, int32_t alpha, int64_t n,
                               int32_t* lvl, int32_t* changed) {
     GRID_STRIDE(i, n) {
         const int2 c = R[i];
@@ -141,7 +141,7 @@ __global__ void k_count_flags(const uint8_t* __restrict__ f, int64_t lo, int64_t
     if ((threadIdx.x & 31) == 0 && s) atomicAdd(out, s);
 }
 
-__global__ void k_level_keys(const int32_t* __restrict__ lvl, int64_t n, uint64_t* key, uint32_t* val) {
+__global__ void k_keys_by_level(const int32_t* __restrict__ lvl, int64_t n, uint64_t* key, uint32_t* val) {
     GRID_STRIDE(i, n) {
         key[i] = (uint64_t)lvl[i];
         val[i] = (uint32_t)i;
@@ -363,7 +363,7 @@ std::unique_ptr<gmr_plan> build_on_device(const gmr_grammar& g, int rows, int co
     for (int64_t round = 0;; ++round) {
         if (round > n + 1) throw Error(GMR_ERR_FORMAT, "device schedule build: levels do not settle");
         GMR_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int32_t), st));
-        LAUNCH(k_level_round, n, 0, R.p, kind.p, alpha, n, lvl.p, flag.p);
+        LAUNCH(k_relax_levels, n, 0, R.p, kind.p, alpha, n, lvl.p, flag.p);
         if (read1(flag.p, st) == 0) break;
     }
     GMR_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int32_t), st));
@@ -424,7 +424,7 @@ std::unique_ptr<gmr_plan> build_on_device(const gmr_grammar& g, int rows, int co
         const auto h = read_n(hist.p, nb, st);
         for (int k = 1; k <= depth; ++k) raw_off[k] = raw_off[k - 1] + (int64_t)h[k];
     }
-    LAUNCH(k_level_keys, n, 0, lvl.p, n, k1, v1);
+    LAUNCH(k_keys_by_level, n, 0, lvl.p, n, k1, v1);
     dev::radix_sort(k1, k2, v1, v2, n, bits_for((uint64_t)depth), tmp.p, st);
     // (3) liveness, deepest level first
     for (int k = depth; k >= 1; --k) {
