@@ -211,6 +211,34 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+class NvmlEnergy:
+    """Total-energy counter of one GPU through NVML (libnvidia-ml, ctypes); the
+    reference measures mJ per vector the same way (gpu_engine.cu NVML replay)."""
+
+    def __init__(self, index: int):
+        import ctypes
+        self.h = None
+        try:
+            self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+            if self.lib.nvmlInit_v2() != 0:
+                return
+            h = ctypes.c_void_p()
+            if self.lib.nvmlDeviceGetHandleByIndex_v2(index, ctypes.byref(h)) != 0:
+                return
+            self.h = h
+        except OSError:
+            self.h = None
+
+    def mj(self):
+        import ctypes
+        if self.h is None:
+            return None
+        e = ctypes.c_ulonglong()
+        if self.lib.nvmlDeviceGetTotalEnergyConsumption(self.h, ctypes.byref(e)) != 0:
+            return None
+        return float(e.value)
+
+
 def measured_peak_hbm():
     p = REPO / "MEASURED_PEAKS.json"
     if p.exists():
@@ -645,6 +673,22 @@ def main():
     ms_per_step = ms / args.steps
     value = ws * B * args.steps / (ms / 1000.0)
 
+    # ---- energy per vector: NVML energy counter around >= 2 s of steps
+    energy = None
+    nv = NvmlEnergy(local)
+    if nv.h is not None:
+        n_e = max(1, int(2000.0 / max(ms_per_step, 1e-3)))
+        torch.cuda.synchronize(dev)
+        e_start, t_start = nv.mj(), time.perf_counter()
+        for _ in range(n_e):
+            step()
+        torch.cuda.synchronize(dev)
+        e_end, t_end = nv.mj(), time.perf_counter()
+        if e_start is not None and e_end is not None and e_end > e_start:
+            joules = (e_end - e_start) / 1000.0
+            energy = {"mj_per_vector": 1000.0 * joules / (n_e * B), "avg_power_w": joules / (t_end - t_start),
+                      "steps": n_e, "how": "NVML total energy counter around the steps (whole GPU)"}
+
     # ---- per-launch times (the same kernels launched one by one) for the roofline
     reps = 5
     lt = np.mean([eng.time_launches(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, variant=args.variant)
@@ -733,6 +777,7 @@ def main():
                 "d2h_bytes_per_step": int(rows * words * 4), "api": "gmr_engine_multiply_host_many (pipelined)",
                 "synchronous_per_call_value": e2e_sync_value},
         "gpu_launches": int(launches_per_step * args.steps),
+        "energy": energy,
         "clocks": clocks,
         "plain_sweep_b1": {"value": plain_vps, "unit": "vectors/s", "speedup": value / ws / plain_vps},
         "grammar": {"ops": st["n_ops"], "depth": st["depth"], "layered_rules": st["ref_layered"],
