@@ -615,6 +615,28 @@ def main():
     def step():
         eng.multiply_device(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, **cfg)
 
+    def step_cfg(**c):
+        eng.multiply_device(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, **c)
+
+    nvml = NvmlEnergy(local)
+
+    def energy_of(fn, seconds=1.5):
+        """mJ per vector of fn() repeated for about `seconds` (NVML energy counter)."""
+        if nvml.h is None:
+            return None
+        fn()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize(dev)
+        n = max(1, int(seconds / max(time.perf_counter() - t0, 1e-5)))
+        e0 = nvml.mj()
+        for _ in range(n):
+            fn()
+        torch.cuda.synchronize(dev)
+        e1 = nvml.mj()
+        return None if e0 is None or e1 is None else (e1 - e0) / (n * B)
+
     def timed(n, **c):
         for _ in range(3):
             eng.multiply_device(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, **c)
@@ -631,6 +653,13 @@ def main():
             tuning["autotuned_table"] = [int(v) for v in eng.level_variants(sr, B)]
             auto_ms = timed(30)
             tuning["autotuned_vps"] = B * 1000.0 / auto_ms
+            tuning["autotuned_mj_per_vector"] = energy_of(lambda: step_cfg(variant=0))
+            # energy-aware table: chunked twins within 10 % of the fastest variant
+            eng.autotune(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, reps=3, energy_tolerance=0.10)
+            tuning["energy_table"] = [int(v) for v in eng.level_variants(sr, B)]
+            tuning["energy_table_vps"] = B * 1000.0 / timed(30)
+            tuning["energy_table_mj_per_vector"] = energy_of(lambda: step_cfg(variant=0))
+            eng.autotune(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, reps=3)
             if learn.MODEL_PATH.exists():
                 model = learn.Mlp.load(learn.MODEL_PATH)
                 t0 = time.perf_counter()
@@ -675,7 +704,7 @@ def main():
 
     # ---- energy per vector: NVML energy counter around >= 2 s of steps
     energy = None
-    nv = NvmlEnergy(local)
+    nv = nvml
     if nv.h is not None:
         n_e = max(1, int(2000.0 / max(ms_per_step, 1e-3)))
         torch.cuda.synchronize(dev)

@@ -1289,9 +1289,23 @@ extern "C" int gmr_engine_get_level_variants(const gmr_engine* e, int semiring, 
     });
 }
 
+extern "C" int gmr_engine_autotune_energy(gmr_engine* e, int semiring, const void* dX, void* dY, int B,
+                                          void* stream, int reps, float tolerance, float* ms, int cap);
+
 extern "C" int gmr_engine_autotune(gmr_engine* e, int semiring, const void* dX, void* dY, int B, void* stream,
                                    int reps, float* ms, int cap) {
+    return gmr_engine_autotune_energy(e, semiring, dX, dY, B, stream, reps, 0.0f, ms, cap);
+}
+
+// Source-chunked variants (v >= 10) fold a level's emissions one L2-sized
+// chunk of sources at a time, so the gathered values come from L2 instead of
+// HBM: the same work with fewer DRAM bytes, hence less energy.  With
+// tolerance > 0 a launch takes the chunked twin of its fastest variant when
+// that is at most (1 + tolerance) times slower.
+extern "C" int gmr_engine_autotune_energy(gmr_engine* e, int semiring, const void* dX, void* dY, int B,
+                                          void* stream, int reps, float tolerance, float* ms, int cap) {
     return guarded([&] {
+        if (tolerance < 0.0f || !(tolerance < 1.0f)) throw Error(GMR_ERR_ARG, "tolerance must be in [0, 1)");
         if (!e) throw Error(GMR_ERR_ARG, "null engine");
         const int nl = e->depth + 2, nv = GMR_N_LEVEL_VARIANTS;
         if (ms && cap < nl * nv) throw Error(GMR_ERR_RANGE, "need room for (depth + 2) x variants times");
@@ -1323,6 +1337,9 @@ extern "C" int gmr_engine_autotune(gmr_engine* e, int semiring, const void* dX, 
             int b = 0;
             for (int v = 1; v < nv; ++v)
                 if (med[(size_t)l * nv + v] < med[(size_t)l * nv + b]) b = v;
+            const int twin = b + 10;  // v = emit + 5 grid + 10 chunked
+            if (tolerance > 0.0f && b < 10 && med[(size_t)l * nv + twin] <= med[(size_t)l * nv + b] * (1.0f + tolerance))
+                b = twin;
             best[l] = (uint8_t)b;
         }
         if (gmr_engine_set_level_variants(e, semiring, B, best.data(), nl) != GMR_OK) throw Error(GMR_ERR_ARG, gmr_last_error());

@@ -507,12 +507,16 @@ class Engine:
                                                    buf.ctypes.data_as(C.POINTER(C.c_uint8)), len(buf), C.byref(n)))
         return buf[: n.value].copy() if n.value else None
 
-    def autotune(self, semiring, x_ptr: int, y_ptr: int, B: int, stream: int = 0, reps: int = 3) -> np.ndarray:
-        """Exhaustive per-launch autotuner; installs the best table and returns times[slot][variant] (ms)."""
+    def autotune(self, semiring, x_ptr: int, y_ptr: int, B: int, stream: int = 0, reps: int = 3,
+                 energy_tolerance: float = 0.0) -> np.ndarray:
+        """Exhaustive per-launch autotuner; installs the best table and returns times[slot][variant] (ms).
+        energy_tolerance > 0 prefers each launch's source-chunked twin (fewer DRAM bytes) when it is at
+        most that fraction slower."""
         depth = self.depth
         ms = np.zeros((depth + 2) * self.N_LEVEL_VARIANTS, dtype=np.float32)
-        _check(lib().gmr_engine_autotune(self._h, semiring_id(semiring), C.c_void_p(x_ptr), C.c_void_p(y_ptr), B,
-                                         C.c_void_p(stream), reps, ms.ctypes.data_as(L.F32P), len(ms)))
+        _check(lib().gmr_engine_autotune_energy(self._h, semiring_id(semiring), C.c_void_p(x_ptr),
+                                                C.c_void_p(y_ptr), B, C.c_void_p(stream), reps,
+                                                float(energy_tolerance), ms.ctypes.data_as(L.F32P), len(ms)))
         return ms.reshape(depth + 2, self.N_LEVEL_VARIANTS)
 
     @property

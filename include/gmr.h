@@ -295,6 +295,14 @@ int gmr_engine_get_level_variants(const gmr_engine* e, int semiring, int B, uint
  * fastest, and writes the times to ms[slot * GMR_N_LEVEL_VARIANTS + v]. */
 int gmr_engine_autotune(gmr_engine* e, int semiring, const void* dX, void* dY, int B,
                         void* stream, int reps, float* ms, int cap);
+/* The same, trading a little time for fewer DRAM bytes: a launch whose
+ * fastest variant is not source-chunked takes its chunked twin when that is at
+ * most (1 + tolerance) times slower (the chunked fold reads the gathered values
+ * from L2; measured on the 200k x 10k grammar at B = 32 with tolerance 0.10:
+ * 1.3 % fewer vectors/s, 10 % less energy per vector).  tolerance = 0 is
+ * gmr_engine_autotune. */
+int gmr_engine_autotune_energy(gmr_engine* e, int semiring, const void* dX, void* dY, int B,
+                               void* stream, int reps, float tolerance, float* ms, int cap);
 /* ------------------------------------------------------------------ */
 /* Learned cost model for the per-launch variant choice                */
 /* ------------------------------------------------------------------ */

@@ -183,6 +183,30 @@ def test_autotuned_and_mixed_tables(case, sr):
     assert eng.level_variants(sr, B) is None
 
 
+@pytest.mark.parametrize("sr", range(3))
+def test_energy_aware_autotune(case, sr):
+    """With a tolerance, each launch takes the chunked twin of its fastest
+    variant when that is within the tolerance; results are unchanged."""
+    torch = pytest.importorskip("torch")
+    rows, cols, B = int(case["rows"]), int(case["cols"]), 32
+    X = random_X(sr, cols, B, 78)
+    ref = oracle_columns(case["sched"], sr, case["V"], X, rows, cols)
+    eng = gmr.Engine(case["plan"])
+    Xw = engine_inputs(sr, X)
+    dX = torch.from_numpy(Xw.view(np.int32)).cuda()
+    dY = torch.empty((rows, Xw.shape[1]), dtype=torch.int32, device="cuda")
+    tol = 0.5
+    times = eng.autotune(sr, dX.data_ptr(), dY.data_ptr(), B, energy_tolerance=tol)
+    table = eng.level_variants(sr, B)
+    for slot in range(1, eng.depth + 2):
+        b = int(times[slot].argmin())
+        want = b + 10 if b < 10 and times[slot, b + 10] <= times[slot, b] * (1 + tol) else b
+        assert table[slot] == want
+    check(sr, engine_outputs(sr, eng.multiply(Xw, sr, B=B), B), ref)
+    with pytest.raises(gmr.GmrError):
+        eng.autotune(sr, dX.data_ptr(), dY.data_ptr(), B, energy_tolerance=1.5)
+
+
 def test_persistent_barrier_timeout_reports_status(c1):
     """A grid-barrier wait limited to one poll gives up: the host gets
     GMR_ERR_TIMEOUT, and the next multiply on the same context is correct."""
