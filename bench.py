@@ -64,6 +64,25 @@ def dist_env():
     return ws, rank, local
 
 
+def slowest_rank_ms(ms: float, ws: int, device=None) -> float:
+    """Length of the timed region on the slowest rank (every rank gets it):
+    a max all-reduce over the process group (NCCL on the GPUs, gloo on CPU)."""
+    if ws <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_vps(ws: int, B: int, steps: int, ms: float) -> float:
+    """Vectors per second of the whole job: every rank multiplies its own B
+    right-hand sides per step (replicas, weak scaling)."""
+    return ws * B * steps / (ms / 1000.0)
+
+
 def cache_dir() -> Path:
     d = Path(os.environ.get("GMR_CACHE_DIR", REPO / "_cache"))
     d.mkdir(parents=True, exist_ok=True)
@@ -694,13 +713,9 @@ def main():
     if ws > 1:
         torch.distributed.barrier()
     clocks = sampler.stop()
-    ms = e0.elapsed_time(e1)
-    if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = slowest_rank_ms(e0.elapsed_time(e1), ws, dev)
     ms_per_step = ms / args.steps
-    value = ws * B * args.steps / (ms / 1000.0)
+    value = whole_job_vps(ws, B, args.steps, ms)
 
     # ---- energy per vector: NVML energy counter around >= 2 s of steps
     energy = None
