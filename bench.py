@@ -306,6 +306,38 @@ def cpu_reference_rate(g, sr, rows, cols, seconds: float, threads: int, gpu_y0=N
     return n / spent, n, spent, build_s, check
 
 
+def reference_gpu_rate(g, sr, rows, cols, Xh, B, device, seconds=1.5):
+    """The reference's own GPU engine on this GPU: its kernels
+    (gpu-engine/gpu_engine.cu, compiled to PTX in oracle/_ref) with its host
+    sequence (restated in oracle/ref/ref_gpu.cpp), single-vector and batched
+    at this B, on the same grammar; returns rates and its first column."""
+    from oracle import oracle as O
+
+    why = O.RefGpu.available()
+    if why:
+        return {"unavailable": why}, None
+    ref = O.RefGpu(device)
+    sched = O.RefSchedule(g.alpha, g.rules(), g.C())
+    V = g.values().astype(np.float32)
+    if sr == 1:  # the reference's Boolean engine takes one 0/1 float per vector
+        Xf = ((Xh[:, :, None] >> np.arange(32, dtype=np.uint32)) & 1).reshape(cols, -1)[:, :B].astype(np.float32)
+    elif sr == 2:
+        Xf = np.minimum(Xh.astype(np.float64), 1e9).astype(np.float32)
+    else:
+        Xf = Xh.astype(np.float32)
+    out = {"how": "the reference's kernels (gpu_engine.cu eval_level_layered / emit_level and the batched ones) "
+                  "in its host sequence, device memory, ms from CUDA events around the iterations"}
+    y0 = None
+    for b, X in ((1, Xf[:, :1]), (B, Xf)):
+        Y, ms = ref.run(sched, sr, V, X, rows, cols, iters=1)
+        iters = max(2, min(200, int(seconds * 1000.0 / max(ms, 1e-3))))
+        Y, ms = ref.run(sched, sr, V, X, rows, cols, iters=iters)
+        out[f"B{b}"] = {"vps": b * 1000.0 / ms, "ms_per_multiply": ms, "iters": iters}
+        if b == B:
+            y0 = Y[:, 0]
+    return out, y0
+
+
 def dtype_of(sr):
     return {0: "f32", 1: "u32 (32 bit-packed OR-AND vectors)", 2: "i32"}[sr]
 
@@ -567,6 +599,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--dump-launches", action="store_true", help="per-launch times and level sizes to stderr")
     ap.add_argument("--no-cusparse", action="store_true", help="skip the cuSPARSE CSR baseline")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip the reference's own GPU engine (plain per-level sweep) baseline")
     ap.add_argument("--op", choices=["right", "left", "fixpoint", "repair"], default="right",
                     help="right: Y = M X (the headline); left: Y = X^T M; fixpoint: X <- X (+) M X to convergence; "
                          "repair: RePair of the workload's matrix on the GPU vs the host")
@@ -836,6 +870,20 @@ def main():
         out["cusparse_csr"] = cusparse_baseline(torch, args, rows, cols, B)
         if out["cusparse_csr"] and "spmm_vps" in out["cusparse_csr"]:
             out["cusparse_csr"]["engine_speedup"] = value / out["cusparse_csr"]["spmm_vps"]
+    if rank == 0 and ws == 1 and not args.no_reference_gpu:
+        yh = Y.cpu().numpy()
+        rg, ry0 = reference_gpu_rate(g, sr, rows, cols, Xh, B, local)
+        if ry0 is not None:
+            ours0 = yh.view(np.float32)[:, 0] if sr == 0 else (
+                (yh.view(np.uint32)[:, 0] & np.uint32(1)).astype(np.int64) if sr == 1 else yh[:, 0])
+            if sr == 0:
+                rg["max_rel_diff_vs_engine"] = float(np.abs(ours0.astype(np.float64) - ry0).max() /
+                                                     max(np.abs(ry0).max(), 1e-30))
+            else:
+                rg["mismatches_vs_engine"] = int(np.sum(np.asarray(ours0, np.int64) != np.asarray(ry0, np.int64)))
+            rg["engine_speedup_same_B"] = value / rg[f"B{B}"]["vps"]
+            rg["engine_speedup_vs_B1"] = value / rg["B1"]["vps"]
+        out["reference_gpu"] = rg
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         yh = Y.cpu().numpy()
         if sr == 0:

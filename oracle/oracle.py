@@ -21,10 +21,20 @@ NAMES = {0: "plustimes", 1: "boolean", 2: "tropical"}
 _lib = None
 
 
+REFGPU_LIB = HERE / "librefgpu.so"
+REFGPU_PTX = HERE / "_ref" / "gpu_engine.ptx"
+
+
 def build(force: bool = False) -> Path:
     src = HERE / "oracle.c"
     if force or not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
         subprocess.run(["make", "-s", "-C", str(HERE), "-B", "liboracle.so"], check=True)
+    lsrc = HERE / "ref" / "ref_gpu.cpp"
+    if force or not REFGPU_LIB.exists() or REFGPU_LIB.stat().st_mtime < lsrc.stat().st_mtime:
+        # the launcher needs the CUDA driver headers; without them the
+        # reference-GPU baseline is simply unavailable
+        subprocess.run(["make", "-s", "-C", str(HERE), "-B", "librefgpu.so"], check=False,
+                       capture_output=True)
     return LIB
 
 
@@ -163,3 +173,63 @@ def brute_force(vc, semiring, V, x, rows, cols) -> np.ndarray:
                           x.ctypes.data_as(C.POINTER(C.c_float)), rows, cols,
                           y.ctypes.data_as(C.POINTER(C.c_double)))
     return y
+
+
+class RefGpu:
+    """The reference's own GPU kernels (gpu-engine/gpu_engine.cu, compiled to
+    PTX in _ref/) run with the reference's host sequence restated in
+    ref/ref_gpu.cpp: the plain per-level sweep of the reference on this GPU.
+    Baseline and test infrastructure only."""
+
+    _lib = None
+
+    @classmethod
+    def available(cls) -> str | None:
+        """None when usable, else why not."""
+        if not REFGPU_PTX.exists():
+            return "the reference engine's device code (oracle/_ref/gpu_engine.ptx) was not built here"
+        if not REFGPU_LIB.exists():
+            return "oracle/librefgpu.so was not built (CUDA driver headers missing)"
+        return None
+
+    def __init__(self, device: int = 0):
+        why = self.available()
+        if why:
+            raise RuntimeError(why)
+        if RefGpu._lib is None:
+            l = C.CDLL(str(REFGPU_LIB))
+            l.refgpu_error.restype = C.c_char_p
+            l.refgpu_open.argtypes = [C.c_char_p, C.c_int]
+            I, F = C.POINTER(C.c_int), C.POINTER(C.c_float)
+            l.refgpu_run.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, I, I, F, C.c_int,
+                                     C.c_int, C.c_int, I, I, I, I, C.c_int, I, I, C.c_int, F, C.c_void_p, C.c_int,
+                                     C.c_int, F]
+            RefGpu._lib = l
+        if RefGpu._lib.refgpu_open(str(REFGPU_PTX).encode(), device) != 0:
+            raise RuntimeError(RefGpu._lib.refgpu_error().decode())
+
+    def run(self, sched: "RefSchedule", semiring: int, V, X, rows: int, cols: int, iters: int = 1):
+        """X: [cols][B] float32 (the reference's batched layout; B = 1 runs the
+        single-vector kernels).  Returns (Y [rows][B], ms per iteration)."""
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        if X.ndim == 1:
+            X = X.reshape(-1, 1)
+        B = X.shape[1]
+        vi, ci = sched.terminal_tables(cols)
+        rules = sched.rules_lrc()
+        Vf = np.ascontiguousarray(V, dtype=np.float32)
+        Y = np.zeros((rows, B), dtype=np.float32 if semiring == PLUS else np.int32)
+        ms = C.c_float()
+        keep = [np.ascontiguousarray(a, dtype=np.int32) for a in
+                (vi, ci, sched.level_offsets, sched.emit_offsets, sched.emit_pos, sched.emit_row,
+                 sched.term_emit_sym, sched.term_emit_row)]
+        rc = RefGpu._lib.refgpu_run(semiring, rows, cols, sched.alpha, sched.num_layered,
+                                    rules.ctypes.data_as(C.c_void_p), _ip(keep[0]), _ip(keep[1]),
+                                    Vf.ctypes.data_as(C.POINTER(C.c_float)), len(Vf), sched.depth,
+                                    sched.max_width, _ip(keep[2]), _ip(keep[3]), _ip(keep[4]), _ip(keep[5]),
+                                    sched.emit_total, _ip(keep[6]), _ip(keep[7]), sched.num_term,
+                                    X.ctypes.data_as(C.POINTER(C.c_float)), Y.ctypes.data_as(C.c_void_p), B,
+                                    int(iters), C.byref(ms))
+        if rc != 0:
+            raise RuntimeError(RefGpu._lib.refgpu_error().decode())
+        return Y, ms.value / iters
