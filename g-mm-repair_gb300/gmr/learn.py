@@ -132,31 +132,43 @@ def choose_learned(eng: Engine, plan: Plan, model: Mlp, semiring, B: int) -> np.
 
 
 # ---------------------------------------------------------------- corpus
-def corpus_specs(n_mosaic: int, n_graph: int, seed0: int = 100):
-    """Seeded grammar specs over the scheduler corpus ranges, scaled to fit one
-    GPU session: mosaics (rows 10k-60k, cols 1k-10k, founders 16-1024,
-    switch rate 1e-3 to 5e-2) and copy-model graphs (nodes 0.2M-1.5M,
-    degree 8-32, copy probability 0.3-0.9)."""
+def corpus_specs(n_mosaic: int, n_graph: int, seed0: int = 100, full: bool = True):
+    """Seeded grammar specs of the scheduler corpus (seeds seed0, seed0+1, ...):
+    mosaics with rows 10k-500k and cols 1k-20k, both log-uniform (rows shrunk
+    so that rows x cols x 1/2 stays below 1.2e9 non-zeros, the size the GPU
+    RePair holds comfortably), founders 16-1024, switch rate 1e-3 to 5e-2;
+    weighted copy-model graphs with 0.2M-16.8M nodes (log-uniform), degree
+    8-32, copy probability 0.3-0.9.  full=False keeps the earlier small ranges
+    (rows 10k-60k, cols 1k-10k, nodes 0.2M-1.5M) for quick runs."""
     specs = []
     for i in range(n_mosaic):
         r = np.random.default_rng(seed0 + i)
-        specs.append(dict(kind="mosaic", seed=seed0 + i, rows=int(r.integers(10_000, 60_001)),
-                          cols=int(r.integers(1_000, 10_001)), founders=int(2 ** r.uniform(4, 10)),
+        if full:
+            rows = int(np.exp(r.uniform(np.log(10_000), np.log(500_000))))
+            cols = int(np.exp(r.uniform(np.log(1_000), np.log(20_000))))
+            rows = int(min(rows, 2.4e9 / cols))
+        else:
+            rows, cols = int(r.integers(10_000, 60_001)), int(r.integers(1_000, 10_001))
+        specs.append(dict(kind="mosaic", seed=seed0 + i, rows=rows, cols=cols, founders=int(2 ** r.uniform(4, 10)),
                           switch=float(10 ** r.uniform(-3, np.log10(5e-2))), mutation=1e-3))
     for i in range(n_graph):
         r = np.random.default_rng(seed0 + 1000 + i)
-        specs.append(dict(kind="graph", seed=seed0 + 1000 + i, nodes=int(r.integers(200_000, 1_500_001)),
+        nodes = (int(np.exp(r.uniform(np.log(200_000), np.log(16_777_216)))) if full
+                 else int(r.integers(200_000, 1_500_001)))
+        specs.append(dict(kind="graph", seed=seed0 + 1000 + i, nodes=nodes,
                           degree=int(r.integers(8, 33)), copy=float(r.uniform(0.3, 0.9))))
     return specs
 
 
-def make_grammar(spec, threads=0):
+def make_grammar(spec, threads=0, device=None):
+    """Grammar of a corpus spec; device = GPU for the RePair compressor (the
+    same grammar as the host compressor)."""
     if spec["kind"] == "mosaic":
         m = gen_mosaic(spec["rows"], spec["cols"], spec["founders"], spec["switch"], spec["mutation"], spec["seed"],
                        threads)
-        return repair(m, threads), spec["rows"], spec["cols"]
+        return repair(m, threads, device=device), spec["rows"], spec["cols"]
     m = gen_copy_graph(spec["nodes"], spec["degree"], spec["copy"], True, spec["seed"], threads)
-    return repair(m, threads), spec["nodes"], spec["nodes"]
+    return repair(m, threads, device=device), spec["nodes"], spec["nodes"]
 
 
 def random_inputs(torch, semiring: int, cols: int, B: int, seed: int):
@@ -231,11 +243,12 @@ def main():
     ap.add_argument("--holdout", type=float, default=0.25)
     ap.add_argument("--Bs", default="1,8,32,128")
     ap.add_argument("--epochs", type=int, default=80)
+    ap.add_argument("--small", action="store_true", help="the earlier small size ranges")
     args = ap.parse_args()
     out = Path(args.out)
     out.mkdir(parents=True, exist_ok=True)
     Bs = [int(b) for b in args.Bs.split(",")]
-    specs = corpus_specs(args.mosaic, args.graph)
+    specs = corpus_specs(args.mosaic, args.graph, full=not args.small)
     rng = np.random.default_rng(7)
     order = rng.permutation(len(specs))
     n_hold = int(round(len(specs) * args.holdout))
@@ -243,8 +256,8 @@ def main():
     rows_tr, rows_te = [], []
     t0 = time.time()
     for gi, spec in enumerate(specs):
-        g, rows, cols = make_grammar(spec)
-        plan = Plan.build(g, rows, cols)
+        g, rows, cols = make_grammar(spec, device=0)
+        plan = Plan.build(g, rows, cols, device=0)
         eng = Engine(plan)
         for sr in (0, 1, 2):
             for B in Bs:
