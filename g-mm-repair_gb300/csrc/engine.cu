@@ -173,6 +173,14 @@ struct SweepArgs {
     int Bt;           // words per slot in one tile
     int G;            // lanes per unit
     int t0;           // first tile of the launch
+    // Direct terminal emissions (graphs, whose terminal table dwarfs X): the
+    // terminal emissions carry codes val * cols + col (em_tcode) and fold
+    // leaf(V[val], X[col]) straight from X; the prologue then fills T only for
+    // the terminals that rules reference (rule_terms).  nullptr: off.
+    const int32_t* em_tcode = nullptr;
+    const int32_t* rule_terms = nullptr;
+    int64_t n_rule_terms = 0;
+    int32_t cols = 0;
 };
 
 struct LevelArgs {
@@ -190,6 +198,8 @@ struct LevelArgs {
     int64_t n_seg;
     int em_blocks;      // blocks [0, em_blocks) fold emissions, the rest evaluate ops
     int em_chunk;       // emissions per lane group (chunked segmented mode)
+    bool direct;        // em_src holds terminal codes (see SweepArgs::em_tcode)
+    bool direct_ops;    // ops' terminal children are codes: -1 zero terminal, -(code + 2)
 };
 
 template <int GLOG>
@@ -215,11 +225,18 @@ struct Values {
     using T = typename S::T;
     const T* arena;
     const T* term;
-    int Bt;
+    const T* X;
+    const float* V;
+    int Bt, ldx;
+    uint32_t cols;
     __device__ __forceinline__ Values(const SweepArgs& a, int tile)
         : arena(static_cast<const T*>(a.arena) + (int64_t)tile * a.n_ops * a.Bt),
           term(static_cast<const T*>(a.T) + (int64_t)tile * a.n_terms * a.Bt),
-          Bt(a.Bt) {}
+          X(static_cast<const T*>(a.X) + (int64_t)tile * a.Bt),
+          V(a.V),
+          Bt(a.Bt),
+          ldx(a.ldx),
+          cols((uint32_t)a.cols) {}
     __device__ __forceinline__ const T* addr(int32_t c, int lane) const {
         const bool slot = c >= 0;
         const int64_t idx = slot ? (int64_t)c : (-(int64_t)c - 1);
@@ -227,6 +244,29 @@ struct Values {
     }
     __device__ __forceinline__ Vec<T, VEC> get(int32_t c, int lane) const {
         return vload_rw<T, VEC, CG>(addr(c, lane));
+    }
+    // leaf(V[val], X[col]) of the terminal with code val * cols + col.
+    __device__ __forceinline__ Vec<T, VEC> leaf_of(uint32_t code, int lane) const {
+        const uint32_t vi = code / cols, col = code - vi * cols;
+        const float v = __ldg(V + vi);
+        const Vec<T, VEC> x = vload<T, VEC>(X + (int64_t)col * ldx + lane * VEC);
+        Vec<T, VEC> out;
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) out.v[j] = S::leaf(v, x.v[j]);
+        return out;
+    }
+    // An emission's value: its reference, or with `direct` a terminal code
+    // (< 0: the zero terminal) evaluated from X.
+    __device__ __forceinline__ Vec<T, VEC> get_em(int32_t c, int lane, bool direct) const {
+        if (!direct) return get(c, lane);
+        if (c < 0) return vzero<S, VEC>();
+        return leaf_of((uint32_t)c, lane);
+    }
+    // A rule child: a slot, the zero terminal (-1), or with `direct` a
+    // terminal code stored as -(code + 2).
+    __device__ __forceinline__ Vec<T, VEC> get_op(int32_t c, int lane, bool direct) const {
+        if (!direct || c >= -1) return get(c, lane);
+        return leaf_of((uint32_t)(-(int64_t)c - 2), lane);
     }
 };
 
@@ -239,14 +279,16 @@ __device__ __forceinline__ T* yptr(const SweepArgs& a, int64_t row, int tile, in
 template <class S, int VEC, int GLOG>
 __device__ __forceinline__ void do_prologue(const SweepArgs& a, int tile, int64_t t0, int64_t stride) {
     using T = typename S::T;
-    const int64_t ny = items_of<GLOG>(a.rows, a.G), nt = items_of<GLOG>(a.n_terms, a.G);
+    const int64_t nq = a.rule_terms ? a.n_rule_terms : a.n_terms;
+    const int64_t ny = items_of<GLOG>(a.rows, a.G), nt = items_of<GLOG>(nq, a.G);
     T* Tt = static_cast<T*>(a.T) + (int64_t)tile * a.n_terms * a.Bt;
     for (int64_t t = t0; t < ny + nt; t += stride) {
         if (t < ny) {
             vstore<T, VEC>(yptr<T>(a, unit_of<GLOG>(t, a.G), tile, lane_of<GLOG>(t, a.G), VEC), vzero<S, VEC>());
         } else {
             const int64_t u = t - ny;
-            const int64_t q = unit_of<GLOG>(u, a.G);
+            const int64_t i = unit_of<GLOG>(u, a.G);
+            const int64_t q = a.rule_terms ? (int64_t)__ldg(a.rule_terms + i) : i;
             const int lane = lane_of<GLOG>(u, a.G);
             Vec<T, VEC> out;
             if (q == 0) {
@@ -284,8 +326,8 @@ __device__ __forceinline__ void do_ops(const SweepArgs& a, const LevelArgs& L, i
         const int64_t sa = L.op_first + unit_of<GLOG>(t, a.G), sb = L.op_first + unit_of<GLOG>(hb ? tb : t, a.G);
         const int la = lane_of<GLOG>(t, a.G), lb = lane_of<GLOG>(hb ? tb : t, a.G);
         const int2 oa = __ldg(L.ops + sa), ob = __ldg(L.ops + sb);
-        Vec<T, VEC> la_v = val.get(oa.x, la), ra_v = val.get(oa.y, la);
-        Vec<T, VEC> lb_v = val.get(ob.x, lb), rb_v = val.get(ob.y, lb);
+        Vec<T, VEC> la_v = val.get_op(oa.x, la, L.direct_ops), ra_v = val.get_op(oa.y, la, L.direct_ops);
+        Vec<T, VEC> lb_v = val.get_op(ob.x, lb, L.direct_ops), rb_v = val.get_op(ob.y, lb, L.direct_ops);
         if (L.op_c) {
             const float ca = __ldg(L.op_c + sa), cb = __ldg(L.op_c + sb);
 #pragma unroll
@@ -310,7 +352,7 @@ __device__ __forceinline__ void do_emits_atomic(const SweepArgs& a, const LevelA
         const int64_t e = L.em_first + unit_of<GLOG>(t, a.G);
         const int lane = lane_of<GLOG>(t, a.G);
         const int32_t src = __ldg(L.em_src + e), row = __ldg(L.em_row + e);
-        vred<S, VEC>(yptr<T>(a, row, tile, lane, VEC), val.get(src, lane));
+        vred<S, VEC>(yptr<T>(a, row, tile, lane, VEC), val.get_em(src, lane, L.direct));
     }
 }
 
@@ -358,7 +400,7 @@ __device__ __forceinline__ void do_emits_warp(const SweepArgs& a, const LevelArg
         const int32_t rb = vb ? __ldg(L.em_row + L.em_first + eb) : -1 - lane;
         const int32_t sa = va ? __ldg(L.em_src + L.em_first + ea) : -1;
         const int32_t sb = vb ? __ldg(L.em_src + L.em_first + eb) : -1;
-        Vec<T, VEC> xa = val.get(sa, 0), xb = val.get(sb, 0);  // ref -1 = the zero terminal
+        Vec<T, VEC> xa = val.get_em(sa, 0, L.direct), xb = val.get_em(sb, 0, L.direct);  // -1: zero
         const unsigned pa = __match_any_sync(0xffffffffu, ra), pb = __match_any_sync(0xffffffffu, rb);
         Vec<T, VEC> ta = warp_segment_reduce<S, VEC>(xa, pa, lane);
         Vec<T, VEC> tb = warp_segment_reduce<S, VEC>(xb, pb, lane);
@@ -394,7 +436,7 @@ __device__ __forceinline__ void do_emits_chunk(const SweepArgs& a, const LevelAr
             }
             Vec<T, VEC> v[4];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) v[j] = val.get(s[j], lane);
+            for (int j = 0; j < 4; ++j) v[j] = val.get_em(s[j], lane, L.direct);
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 if (r[j] != cur) {
@@ -408,7 +450,7 @@ __device__ __forceinline__ void do_emits_chunk(const SweepArgs& a, const LevelAr
         }
         for (; e < e1; ++e) {
             const int32_t r = __ldg(rows + e);
-            Vec<T, VEC> v = val.get(__ldg(srcs + e), lane);
+            Vec<T, VEC> v = val.get_em(__ldg(srcs + e), lane, L.direct);
             if (r != cur) {
                 vred<S, VEC>(yptr<T>(a, cur, tile, lane, VEC), acc);
                 acc = v;
@@ -441,12 +483,12 @@ __device__ __forceinline__ void do_emits_rows(const SweepArgs& a, const LevelArg
         for (; e + 4 <= e1; e += 4) {
             const int32_t s0 = __ldg(L.em_src + e), s1 = __ldg(L.em_src + e + 1);
             const int32_t s2 = __ldg(L.em_src + e + 2), s3 = __ldg(L.em_src + e + 3);
-            Vec<T, VEC> v0 = val.get(s0, lane), v1 = val.get(s1, lane);
-            Vec<T, VEC> v2 = val.get(s2, lane), v3 = val.get(s3, lane);
+            Vec<T, VEC> v0 = val.get_em(s0, lane, L.direct), v1 = val.get_em(s1, lane, L.direct);
+            Vec<T, VEC> v2 = val.get_em(s2, lane, L.direct), v3 = val.get_em(s3, lane, L.direct);
             acc0 = voplus<S, VEC>(acc0, voplus<S, VEC>(v0, v1));
             acc1 = voplus<S, VEC>(acc1, voplus<S, VEC>(v2, v3));
         }
-        for (; e < e1; ++e) acc0 = voplus<S, VEC>(acc0, val.get(__ldg(L.em_src + e), lane));
+        for (; e < e1; ++e) acc0 = voplus<S, VEC>(acc0, val.get_em(__ldg(L.em_src + e), lane, L.direct));
         T* yp = yptr<T>(a, row, tile, lane, VEC);
         vstore<T, VEC>(yp, voplus<S, VEC>(vload_rw<T, VEC, CG>(yp), voplus<S, VEC>(acc0, acc1)));
     }
@@ -535,6 +577,8 @@ __global__ void __launch_bounds__(256) k_persistent(SweepArgs a, LevelArgs L0, P
         L.n_em = P.em_off[k] - P.em_off[k - 1];
         L.seg_first = P.seg_off[k - 1];
         L.n_seg = P.seg_off[k] - P.seg_off[k - 1];
+        L.direct = k == 1 && a.em_tcode != nullptr;
+        if (L.direct) L.em_src = a.em_tcode;
         if constexpr (EMIT == GMR_EMIT_ATOMIC) do_emits_atomic<S, VEC, GLOG, true>(a, L, 0, t0, stride);
         else if constexpr (EMIT == GMR_EMIT_ROWS) do_emits_rows<S, VEC, GLOG, true>(a, L, 0, t0, stride);
         else if constexpr (GLOG == 0) do_emits_warp<S, VEC, true>(a, L, 0, t0, stride);
@@ -604,6 +648,11 @@ struct gmr_engine {
     gmr::DevBuf em_src_c, em_row_c, seg_row_c, seg_start_c;
     std::vector<int64_t> ch_off, ch_em, ch_seg;
     bool chunked = false;
+    // Direct terminal emissions (SweepArgs::em_tcode): codes of the terminal
+    // emissions and the terminals rules reference.
+    gmr::DevBuf em_tcode, rule_terms, ops_direct;
+    int64_t n_rule_terms = 0;
+    bool direct_terms = false;
     // Left product (y = x^T M): flat edge lists uploaded by gmr_engine_enable_left.
     gmr::DevBuf le_src, le_tgt, le_split, tcol_off, tcol_q;
     std::vector<int64_t> le_off;
@@ -620,7 +669,7 @@ struct gmr_engine {
     std::vector<gmr::DevBuf*> schedule_bufs() {
         return {&ops, &op_c, &em_src, &em_row, &seg_row, &seg_start, &term_val, &term_col, &V,
                 &d_lvl_off, &d_em_off, &d_seg_off, &sync, &em_src_c, &em_row_c, &seg_row_c, &seg_start_c,
-                &le_src, &le_tgt, &le_split, &tcol_off, &tcol_q};
+                &le_src, &le_tgt, &le_split, &tcol_off, &tcol_q, &em_tcode, &rule_terms, &ops_direct};
     }
 };
 
@@ -646,6 +695,15 @@ struct LaunchTimer {
 };
 static thread_local LaunchTimer* t_timer = nullptr;
 
+// Direct terminal emissions on: the sweep's terminal emissions gather X.
+static void set_direct(const gmr_engine* e, SweepArgs& a) {
+    a.cols = e->cols;
+    if (!e->direct_terms) return;
+    a.em_tcode = static_cast<const int32_t*>(e->em_tcode.p);
+    a.rule_terms = static_cast<const int32_t*>(e->rule_terms.p);
+    a.n_rule_terms = e->n_rule_terms;
+}
+
 template <class S, int VEC, int GLOG>
 static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void* Y, cudaStream_t st,
                            int64_t& launches) {
@@ -667,6 +725,7 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
     a.Bt = lc.Bt;
     a.G = lc.G;
     a.t0 = 0;
+    set_direct(e, a);
     const int TPB = 256;
     auto blocks_for = [&](int64_t items, int nt) -> int {
         int64_t b = (items + TPB - 1) / TPB;
@@ -678,7 +737,7 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
         if (t_timer && mark) t_timer->mark();
     };
     {
-        int64_t items = (e->rows + e->n_terms) * (int64_t)lc.G;
+        int64_t items = (e->rows + (e->direct_terms ? e->n_rule_terms : e->n_terms)) * (int64_t)lc.G;
         dim3 grid(blocks_for(items, lc.ntile), lc.ntile);
         k_prologue<S, VEC, GLOG><<<grid, TPB, 0, st>>>(a);
         after();
@@ -688,7 +747,8 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
         SweepArgs s = a;
         s.t0 = t0;
         LevelArgs L{};
-        L.ops = static_cast<const int2*>(e->ops.p);
+        L.ops = static_cast<const int2*>(e->direct_terms ? e->ops_direct.p : e->ops.p);
+        L.direct_ops = e->direct_terms;
         L.op_c = e->has_coeff ? static_cast<const float*>(e->op_c.p) : nullptr;
         L.em_src = static_cast<const int32_t*>(e->em_src.p);
         L.em_row = static_cast<const int32_t*>(e->em_row.p);
@@ -705,6 +765,11 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
             by_chunk = v >= 2 * kNumEmitVariants;
         }
         if (lc.variant == GMR_VARIANT_PLAIN) emit = GMR_EMIT_ATOMIC;
+        if (k_em == 0 && e->direct_terms) {  // terminal emissions fold leaf(V, X) directly
+            L.em_src = static_cast<const int32_t*>(e->em_tcode.p);
+            L.direct = true;
+            by_chunk = false;
+        }
         if (chunk <= 0) chunk = 16;
         L.em_chunk = chunk;
         int64_t nops = 0, nem = 0, nseg = 0;
@@ -822,8 +887,10 @@ static void launch_persistent_t(gmr_engine* e, const Launch& lc, const void* X, 
     a.Bt = lc.Bt;
     a.G = lc.G;
     a.t0 = 0;
+    set_direct(e, a);
     LevelArgs L{};
-    L.ops = static_cast<const int2*>(e->ops.p);
+    L.ops = static_cast<const int2*>(e->direct_terms ? e->ops_direct.p : e->ops.p);
+    L.direct_ops = e->direct_terms;
     L.op_c = e->has_coeff ? static_cast<const float*>(e->op_c.p) : nullptr;
     L.em_src = static_cast<const int32_t*>(e->em_src.p);
     L.em_row = static_cast<const int32_t*>(e->em_row.p);
@@ -1098,6 +1165,39 @@ static void build_chunked_emissions(const gmr_plan& p, gmr_engine& e) {
     e.chunked = true;
 }
 
+// Direct terminal emissions pay off when the terminal table is much larger
+// than X (graphs: one terminal per (weight, column)), so that gathering
+// X[col] (small, L2-resident) beats gathering T[q]: terminal emissions and
+// rule children then evaluate leaf(V, X[col]) in place and the prologue no
+// longer fills T.  GMR_DIRECT_TERMS=0 / 1 forces the choice.
+static void build_direct_terms(const gmr_plan& p, gmr_engine& e) {
+    const int64_t n_te = p.em_off.size() > 1 ? p.em_off[1] - p.em_off[0] : 0;
+    bool on = n_te > 0 && p.n_terms() > 4 * (int64_t)p.cols;
+    if (const char* f = std::getenv("GMR_DIRECT_TERMS")) on = n_te > 0 && std::atoi(f) != 0;
+    if ((int64_t)p.V.size() * p.cols > INT32_MAX) on = false;  // codes must fit int32
+    e.direct_terms = on;
+    if (!on) return;
+    std::vector<int32_t> code((size_t)n_te);
+    for (int64_t i = 0; i < n_te; ++i) {
+        const int64_t q = -(int64_t)p.em_src[p.em_off[0] + i] - 1;  // >= 1: terminal emissions
+        code[i] = (int32_t)((int64_t)p.term_val[q - 1] * p.cols + p.term_col[q - 1]);
+    }
+    upload(code, e.em_tcode);
+    // rule children: terminals as codes too, so that T keeps only the zero
+    // terminal T[0] (still read by the warp fold's idle lanes)
+    auto enc = [&](int32_t c) -> int32_t {
+        if (c >= -1) return c;
+        const int64_t q = -(int64_t)c - 1;
+        return (int32_t)(-((int64_t)p.term_val[q - 1] * p.cols + p.term_col[q - 1]) - 2);
+    };
+    std::vector<int2> ops((size_t)p.n_ops());
+    for (int64_t i = 0; i < p.n_ops(); ++i) ops[i] = make_int2(enc(p.op_l[i]), enc(p.op_r[i]));
+    upload(ops, e.ops_direct);
+    std::vector<int32_t> list{0};
+    e.n_rule_terms = 1;
+    upload(list, e.rule_terms);
+}
+
 extern "C" int gmr_engine_create(const gmr_plan* p, int device, gmr_engine** out) {
     return guarded([&] {
         if (!p || !out) throw Error(GMR_ERR_ARG, "null argument");
@@ -1137,6 +1237,7 @@ extern "C" int gmr_engine_create(const gmr_plan* p, int device, gmr_engine** out
             std::memset(e->status_host, 0, 16);
             upload(p->term_col, e->term_col);
             upload(p->V, e->V);
+            build_direct_terms(*p, *e);
             GMR_CUDA(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking));
             GMR_CUDA(cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, device));
         } catch (...) {

@@ -117,6 +117,29 @@ def test_golden_batched(case, sr, B):
 
 
 @pytest.mark.parametrize("sr", range(3))
+@pytest.mark.parametrize("B", [1, 5, 32, 40])
+def test_direct_terminal_emissions(case, sr, B, monkeypatch):
+    """Terminal emissions folded as leaf(V, X[col]) straight from X (the mode
+    the engine picks when the terminal table dwarfs X), forced on: every
+    variant, the per-launch tables (chunked ones included) and the
+    persistent kernel still match the oracle."""
+    monkeypatch.setenv("GMR_DIRECT_TERMS", "1")
+    rows, cols = int(case["rows"]), int(case["cols"])
+    X = random_X(sr, cols, B, 500 + B)
+    ref = oracle_columns(case["sched"], sr, case["V"], X, rows, cols)
+    eng = gmr.Engine(case["plan"])
+    Xw = engine_inputs(sr, X)
+    for cfg in CONFIGS:
+        check(sr, engine_outputs(sr, eng.multiply(Xw, sr, B=B, **cfg), B), ref)
+    rng = np.random.default_rng(B)
+    for table in ([v] * (eng.depth + 2) for v in (0, 3, 4, 10, 13)):
+        eng.set_level_variants(sr, B, table)
+        check(sr, engine_outputs(sr, eng.multiply(Xw, sr, B=B), B), ref)
+    eng.set_level_variants(sr, B, rng.integers(0, eng.N_LEVEL_VARIANTS, eng.depth + 2))
+    check(sr, engine_outputs(sr, eng.multiply(Xw, sr, B=B), B), ref)
+
+
+@pytest.mark.parametrize("sr", range(3))
 def test_device_pointers_and_stream(case, sr):
     torch = pytest.importorskip("torch")
     rows, cols, B = int(case["rows"]), int(case["cols"]), 8
