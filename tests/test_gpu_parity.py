@@ -139,6 +139,27 @@ def test_direct_terminal_emissions(case, sr, B, monkeypatch):
     check(sr, engine_outputs(sr, eng.multiply(Xw, sr, B=B), B), ref)
 
 
+@pytest.fixture(scope="module")
+def wgraph():
+    """Weighted copy graph whose terminal table is over 4x its column count,
+    so the engine picks direct terminals by itself."""
+    m = gmr.gen_copy_graph(30000, 24, 0.7, True, 21)
+    g = gmr.repair(m)
+    plan = gmr.Plan.build(g, 30000, 30000)
+    assert plan.stats["n_terms"] > 4 * 30000
+    return dict(g=g, plan=plan, sched=O.RefSchedule(g.alpha, g.rules(), g.C()), V=g.values())
+
+
+@pytest.mark.parametrize("sr,B", [(1, 32), (1, 1), (2, 1), (2, 3), (0, 4)])
+def test_graph_direct_terminals_auto(wgraph, sr, B):
+    X = random_X(sr, 30000, B, 900 + B)
+    ref = oracle_columns(wgraph["sched"], sr, wgraph["V"], X, 30000, 30000)
+    eng = gmr.Engine(wgraph["plan"])
+    for cfg in (dict(variant=gmr.VARIANT_GRAPH), dict(variant=gmr.VARIANT_PLAIN),
+                dict(variant=gmr.VARIANT_PERSISTENT)):
+        check(sr, engine_outputs(sr, eng.multiply(engine_inputs(sr, X), sr, B=B, **cfg), B), ref)
+
+
 @pytest.mark.parametrize("sr", range(3))
 def test_device_pointers_and_stream(case, sr):
     torch = pytest.importorskip("torch")
