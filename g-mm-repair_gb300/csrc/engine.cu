@@ -255,18 +255,27 @@ struct Values {
         for (int j = 0; j < VEC; ++j) out.v[j] = S::leaf(v, x.v[j]);
         return out;
     }
-    // An emission's value: its reference, or with `direct` a terminal code
+    // An emission's value: its reference, or with DIRECT a terminal code
     // (< 0: the zero terminal) evaluated from X.
-    __device__ __forceinline__ Vec<T, VEC> get_em(int32_t c, int lane, bool direct) const {
-        if (!direct) return get(c, lane);
-        if (c < 0) return vzero<S, VEC>();
-        return leaf_of((uint32_t)c, lane);
+    template <bool DIRECT>
+    __device__ __forceinline__ Vec<T, VEC> get_em(int32_t c, int lane) const {
+        if constexpr (!DIRECT) {
+            return get(c, lane);
+        } else {
+            if (c < 0) return vzero<S, VEC>();
+            return leaf_of((uint32_t)c, lane);
+        }
     }
-    // A rule child: a slot, the zero terminal (-1), or with `direct` a
+    // A rule child: a slot, the zero terminal (-1), or with DIRECT a
     // terminal code stored as -(code + 2).
-    __device__ __forceinline__ Vec<T, VEC> get_op(int32_t c, int lane, bool direct) const {
-        if (!direct || c >= -1) return get(c, lane);
-        return leaf_of((uint32_t)(-(int64_t)c - 2), lane);
+    template <bool DIRECT>
+    __device__ __forceinline__ Vec<T, VEC> get_op(int32_t c, int lane) const {
+        if constexpr (!DIRECT) {
+            return get(c, lane);
+        } else {
+            if (c >= -1) return get(c, lane);
+            return leaf_of((uint32_t)(-(int64_t)c - 2), lane);
+        }
     }
 };
 
@@ -313,7 +322,7 @@ __global__ void __launch_bounds__(256) k_prologue(SweepArgs a) {
 }
 
 // Evaluate the ops of one level, two items per thread in flight.
-template <class S, int VEC, int GLOG, bool CG = false>
+template <class S, int VEC, int GLOG, bool CG = false, bool DIR = false>
 __device__ __forceinline__ void do_ops(const SweepArgs& a, const LevelArgs& L, int tile, int64_t t0,
                                        int64_t stride) {
     using T = typename S::T;
@@ -326,8 +335,8 @@ __device__ __forceinline__ void do_ops(const SweepArgs& a, const LevelArgs& L, i
         const int64_t sa = L.op_first + unit_of<GLOG>(t, a.G), sb = L.op_first + unit_of<GLOG>(hb ? tb : t, a.G);
         const int la = lane_of<GLOG>(t, a.G), lb = lane_of<GLOG>(hb ? tb : t, a.G);
         const int2 oa = __ldg(L.ops + sa), ob = __ldg(L.ops + sb);
-        Vec<T, VEC> la_v = val.get_op(oa.x, la, L.direct_ops), ra_v = val.get_op(oa.y, la, L.direct_ops);
-        Vec<T, VEC> lb_v = val.get_op(ob.x, lb, L.direct_ops), rb_v = val.get_op(ob.y, lb, L.direct_ops);
+        Vec<T, VEC> la_v = val.template get_op<DIR>(oa.x, la), ra_v = val.template get_op<DIR>(oa.y, la);
+        Vec<T, VEC> lb_v = val.template get_op<DIR>(ob.x, lb), rb_v = val.template get_op<DIR>(ob.y, lb);
         if (L.op_c) {
             const float ca = __ldg(L.op_c + sa), cb = __ldg(L.op_c + sb);
 #pragma unroll
@@ -342,7 +351,7 @@ __device__ __forceinline__ void do_ops(const SweepArgs& a, const LevelArgs& L, i
 }
 
 // One atomic per (emission, word): the reference's emit scheme.
-template <class S, int VEC, int GLOG, bool CG = false>
+template <class S, int VEC, int GLOG, bool CG = false, bool DIR = false>
 __device__ __forceinline__ void do_emits_atomic(const SweepArgs& a, const LevelArgs& L, int tile, int64_t t0,
                                                 int64_t stride) {
     using T = typename S::T;
@@ -352,7 +361,7 @@ __device__ __forceinline__ void do_emits_atomic(const SweepArgs& a, const LevelA
         const int64_t e = L.em_first + unit_of<GLOG>(t, a.G);
         const int lane = lane_of<GLOG>(t, a.G);
         const int32_t src = __ldg(L.em_src + e), row = __ldg(L.em_row + e);
-        vred<S, VEC>(yptr<T>(a, row, tile, lane, VEC), val.get_em(src, lane, L.direct));
+        vred<S, VEC>(yptr<T>(a, row, tile, lane, VEC), val.template get_em<DIR>(src, lane));
     }
 }
 
@@ -386,7 +395,7 @@ __device__ __forceinline__ Vec<typename S::T, VEC> warp_segment_reduce(Vec<typen
     return tot;
 }
 
-template <class S, int VEC, bool CG = false>
+template <class S, int VEC, bool CG = false, bool DIR = false>
 __device__ __forceinline__ void do_emits_warp(const SweepArgs& a, const LevelArgs& L, int tile, int64_t t0,
                                               int64_t stride) {
     using T = typename S::T;
@@ -400,7 +409,7 @@ __device__ __forceinline__ void do_emits_warp(const SweepArgs& a, const LevelArg
         const int32_t rb = vb ? __ldg(L.em_row + L.em_first + eb) : -1 - lane;
         const int32_t sa = va ? __ldg(L.em_src + L.em_first + ea) : -1;
         const int32_t sb = vb ? __ldg(L.em_src + L.em_first + eb) : -1;
-        Vec<T, VEC> xa = val.get_em(sa, 0, L.direct), xb = val.get_em(sb, 0, L.direct);  // -1: zero
+        Vec<T, VEC> xa = val.template get_em<DIR>(sa, 0), xb = val.template get_em<DIR>(sb, 0);  // -1: zero
         const unsigned pa = __match_any_sync(0xffffffffu, ra), pb = __match_any_sync(0xffffffffu, rb);
         Vec<T, VEC> ta = warp_segment_reduce<S, VEC>(xa, pa, lane);
         Vec<T, VEC> tb = warp_segment_reduce<S, VEC>(xb, pb, lane);
@@ -411,7 +420,7 @@ __device__ __forceinline__ void do_emits_warp(const SweepArgs& a, const LevelArg
 
 // Chunked segmented emits: each lane group walks em_chunk consecutive
 // emissions (loads four ahead), accumulating while the row stays the same.
-template <class S, int VEC, int GLOG, bool CG = false>
+template <class S, int VEC, int GLOG, bool CG = false, bool DIR = false>
 __device__ __forceinline__ void do_emits_chunk(const SweepArgs& a, const LevelArgs& L, int tile, int64_t t0,
                                                int64_t stride) {
     using T = typename S::T;
@@ -436,7 +445,7 @@ __device__ __forceinline__ void do_emits_chunk(const SweepArgs& a, const LevelAr
             }
             Vec<T, VEC> v[4];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) v[j] = val.get_em(s[j], lane, L.direct);
+            for (int j = 0; j < 4; ++j) v[j] = val.template get_em<DIR>(s[j], lane);
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 if (r[j] != cur) {
@@ -450,7 +459,7 @@ __device__ __forceinline__ void do_emits_chunk(const SweepArgs& a, const LevelAr
         }
         for (; e < e1; ++e) {
             const int32_t r = __ldg(rows + e);
-            Vec<T, VEC> v = val.get_em(__ldg(srcs + e), lane, L.direct);
+            Vec<T, VEC> v = val.template get_em<DIR>(__ldg(srcs + e), lane);
             if (r != cur) {
                 vred<S, VEC>(yptr<T>(a, cur, tile, lane, VEC), acc);
                 acc = v;
@@ -467,7 +476,7 @@ __device__ __forceinline__ void do_emits_chunk(const SweepArgs& a, const LevelAr
 // updates its row of Y with a plain read-modify-write.  Within a launch every
 // (row, tile) belongs to exactly one segment and levels are separate launches,
 // so no atomics are needed and the (+,x) summation order is fixed.
-template <class S, int VEC, int GLOG, bool CG = false>
+template <class S, int VEC, int GLOG, bool CG = false, bool DIR = false>
 __device__ __forceinline__ void do_emits_rows(const SweepArgs& a, const LevelArgs& L, int tile, int64_t t0,
                                               int64_t stride) {
     using T = typename S::T;
@@ -483,32 +492,42 @@ __device__ __forceinline__ void do_emits_rows(const SweepArgs& a, const LevelArg
         for (; e + 4 <= e1; e += 4) {
             const int32_t s0 = __ldg(L.em_src + e), s1 = __ldg(L.em_src + e + 1);
             const int32_t s2 = __ldg(L.em_src + e + 2), s3 = __ldg(L.em_src + e + 3);
-            Vec<T, VEC> v0 = val.get_em(s0, lane, L.direct), v1 = val.get_em(s1, lane, L.direct);
-            Vec<T, VEC> v2 = val.get_em(s2, lane, L.direct), v3 = val.get_em(s3, lane, L.direct);
+            Vec<T, VEC> v0 = val.template get_em<DIR>(s0, lane), v1 = val.template get_em<DIR>(s1, lane);
+            Vec<T, VEC> v2 = val.template get_em<DIR>(s2, lane), v3 = val.template get_em<DIR>(s3, lane);
             acc0 = voplus<S, VEC>(acc0, voplus<S, VEC>(v0, v1));
             acc1 = voplus<S, VEC>(acc1, voplus<S, VEC>(v2, v3));
         }
-        for (; e < e1; ++e) acc0 = voplus<S, VEC>(acc0, val.get_em(__ldg(L.em_src + e), lane, L.direct));
+        for (; e < e1; ++e) acc0 = voplus<S, VEC>(acc0, val.template get_em<DIR>(__ldg(L.em_src + e), lane));
         T* yp = yptr<T>(a, row, tile, lane, VEC);
         vstore<T, VEC>(yp, voplus<S, VEC>(vload_rw<T, VEC, CG>(yp), voplus<S, VEC>(acc0, acc1)));
     }
 }
 
+// Emission fold of one launch; DIR: the sources are terminal codes (see
+// SweepArgs::em_tcode).  A compile-time choice, so each fold keeps its batched
+// loads free of per-item branches.
+template <class S, int VEC, int GLOG, int EMIT, bool CG, bool DIR>
+__device__ __forceinline__ void emits_t(const SweepArgs& a, const LevelArgs& L, int tile, int64_t t0, int64_t stride) {
+    if constexpr (EMIT == GMR_EMIT_ATOMIC) do_emits_atomic<S, VEC, GLOG, CG, DIR>(a, L, tile, t0, stride);
+    else if constexpr (EMIT == GMR_EMIT_ROWS) do_emits_rows<S, VEC, GLOG, CG, DIR>(a, L, tile, t0, stride);
+    else if constexpr (GLOG == 0) do_emits_warp<S, VEC, CG, DIR>(a, L, tile, t0, stride);
+    else do_emits_chunk<S, VEC, GLOG, CG, DIR>(a, L, tile, t0, stride);
+}
+
 // One level launch: blocks [0, em_blocks) fold emissions, the rest evaluate ops.
-template <class S, int VEC, int GLOG, int EMIT>
+// DIRK (direct terminals): 0 off; 1 rule children are terminal codes; 2 the
+// emissions too (the launch that folds the terminal emissions).
+template <class S, int VEC, int GLOG, int EMIT, int DIRK = 0>
 __global__ void __launch_bounds__(256) k_level(SweepArgs a, LevelArgs L) {
     const int tile = a.t0 + blockIdx.y;
     if ((int)blockIdx.x < L.em_blocks) {
         const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
         const int64_t stride = (int64_t)L.em_blocks * blockDim.x;
-        if constexpr (EMIT == GMR_EMIT_ATOMIC) do_emits_atomic<S, VEC, GLOG>(a, L, tile, t0, stride);
-        else if constexpr (EMIT == GMR_EMIT_ROWS) do_emits_rows<S, VEC, GLOG>(a, L, tile, t0, stride);
-        else if constexpr (GLOG == 0) do_emits_warp<S, VEC>(a, L, tile, t0, stride);
-        else do_emits_chunk<S, VEC, GLOG>(a, L, tile, t0, stride);
+        emits_t<S, VEC, GLOG, EMIT, false, DIRK == 2>(a, L, tile, t0, stride);
     } else {
         const int64_t t0 = (int64_t)(blockIdx.x - L.em_blocks) * blockDim.x + threadIdx.x;
         const int64_t stride = (int64_t)(gridDim.x - L.em_blocks) * blockDim.x;
-        do_ops<S, VEC, GLOG>(a, L, tile, t0, stride);
+        do_ops<S, VEC, GLOG, false, DIRK >= 1>(a, L, tile, t0, stride);
     }
 }
 
@@ -577,13 +596,8 @@ __global__ void __launch_bounds__(256) k_persistent(SweepArgs a, LevelArgs L0, P
         L.n_em = P.em_off[k] - P.em_off[k - 1];
         L.seg_first = P.seg_off[k - 1];
         L.n_seg = P.seg_off[k] - P.seg_off[k - 1];
-        L.direct = k == 1 && a.em_tcode != nullptr;
-        if (L.direct) L.em_src = a.em_tcode;
-        if constexpr (EMIT == GMR_EMIT_ATOMIC) do_emits_atomic<S, VEC, GLOG, true>(a, L, 0, t0, stride);
-        else if constexpr (EMIT == GMR_EMIT_ROWS) do_emits_rows<S, VEC, GLOG, true>(a, L, 0, t0, stride);
-        else if constexpr (GLOG == 0) do_emits_warp<S, VEC, true>(a, L, 0, t0, stride);
-        else do_emits_chunk<S, VEC, GLOG, true>(a, L, 0, t0, stride);
-        do_ops<S, VEC, GLOG, true>(a, L, 0, t0, stride);
+        emits_t<S, VEC, GLOG, EMIT, true, false>(a, L, 0, t0, stride);
+        do_ops<S, VEC, GLOG, true, false>(a, L, 0, t0, stride);
         if (!grid_barrier(P, k)) return;
     }
 }
@@ -695,6 +709,16 @@ struct LaunchTimer {
 };
 static thread_local LaunchTimer* t_timer = nullptr;
 
+template <class S, int VEC, int GLOG, int DIRK>
+static void launch_level(int emit, dim3 grid, cudaStream_t st, const SweepArgs& s, const LevelArgs& M) {
+    if (emit == GMR_EMIT_ATOMIC)
+        k_level<S, VEC, GLOG, GMR_EMIT_ATOMIC, DIRK><<<grid, 256, 0, st>>>(s, M);
+    else if (emit == GMR_EMIT_ROWS)
+        k_level<S, VEC, GLOG, GMR_EMIT_ROWS, DIRK><<<grid, 256, 0, st>>>(s, M);
+    else
+        k_level<S, VEC, GLOG, GMR_EMIT_SEGMENTED, DIRK><<<grid, 256, 0, st>>>(s, M);
+}
+
 // Direct terminal emissions on: the sweep's terminal emissions gather X.
 static void set_direct(const gmr_engine* e, SweepArgs& a) {
     a.cols = e->cols;
@@ -803,12 +827,10 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
                                             std::max(1, e->sm_count * ops_cap / nt)) : 0;
             M.em_blocks = eb;
             dim3 grid(eb + ob, nt);
-            if (emit == GMR_EMIT_ATOMIC)
-                k_level<S, VEC, GLOG, GMR_EMIT_ATOMIC><<<grid, TPB, 0, st>>>(s, M);
-            else if (emit == GMR_EMIT_ROWS)
-                k_level<S, VEC, GLOG, GMR_EMIT_ROWS><<<grid, TPB, 0, st>>>(s, M);
-            else
-                k_level<S, VEC, GLOG, GMR_EMIT_SEGMENTED><<<grid, TPB, 0, st>>>(s, M);
+            const int dirk = !M.direct_ops ? 0 : M.direct ? 2 : 1;
+            if (dirk == 0) launch_level<S, VEC, GLOG, 0>(emit, grid, st, s, M);
+            else if (dirk == 1) launch_level<S, VEC, GLOG, 1>(emit, grid, st, s, M);
+            else launch_level<S, VEC, GLOG, 2>(emit, grid, st, s, M);
             after(mark);
         };
         if (split) {  // plain: emissions and ops in separate launches
@@ -887,10 +909,8 @@ static void launch_persistent_t(gmr_engine* e, const Launch& lc, const void* X, 
     a.Bt = lc.Bt;
     a.G = lc.G;
     a.t0 = 0;
-    set_direct(e, a);
     LevelArgs L{};
-    L.ops = static_cast<const int2*>(e->direct_terms ? e->ops_direct.p : e->ops.p);
-    L.direct_ops = e->direct_terms;
+    L.ops = static_cast<const int2*>(e->ops.p);
     L.op_c = e->has_coeff ? static_cast<const float*>(e->op_c.p) : nullptr;
     L.em_src = static_cast<const int32_t*>(e->em_src.p);
     L.em_row = static_cast<const int32_t*>(e->em_row.p);
@@ -983,6 +1003,9 @@ static Launch resolve_launch(gmr_engine* e, int semiring, int B, const void* X, 
     lc.Bw = words_per_slot(semiring, B);
     const int asked = cfg ? cfg->variant : GMR_VARIANT_AUTO;
     lc.variant = asked == GMR_VARIANT_AUTO ? GMR_VARIANT_GRAPH : asked;
+    // the persistent kernel reads terminals from T only: with direct terminals
+    // (T holds just the zero terminal) the per-level graph runs instead
+    if (lc.variant == GMR_VARIANT_PERSISTENT && e->direct_terms) lc.variant = GMR_VARIANT_GRAPH;
     lc.spin_limit = cfg && cfg->spin_limit > 0 ? (unsigned long long)cfg->spin_limit : 20000000ull;
     if (asked == GMR_VARIANT_AUTO && !(cfg && cfg->emit_mode)) {
         auto it = e->level_variants.find({semiring, B});

@@ -67,8 +67,10 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         jobs.append(["g++", *common, "-fPIC", "-Wall", "-pthread", "-c", str(CSRC / s),
                      "-o", str(BUILD / (s + ".o"))])
     for s in CUDA_SOURCES:
-        jobs.append([nvcc, *ARCH, "-lineinfo", *common, "-Xcompiler", "-fPIC", "-c", str(CSRC / s),
-                     "-o", str(BUILD / (s + ".o"))])
+        # --split-compile=0: device optimisation in parallel threads (engine.cu
+        # instantiates many kernel variants)
+        jobs.append([nvcc, *ARCH, "-lineinfo", "--split-compile=0", *common, "-Xcompiler", "-fPIC", "-c",
+                     str(CSRC / s), "-o", str(BUILD / (s + ".o"))])
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         for r in ex.map(_run, jobs):
             if verbose and (r.stdout or r.stderr):
