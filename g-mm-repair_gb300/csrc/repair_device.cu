@@ -6,6 +6,9 @@
 //      second pair of a run "aaa" (RePair counts non-overlapping ones): a
 //      pair inside a run of equal symbols is counted when its distance to the
 //      run's first symbol is even (run starts by a running-maximum scan);
+//      after the first round only pairs that hold a symbol of the previous
+//      round or were candidates then can reach a count of two, and only they
+//      go on (a compaction);
 //   2. one stable radix sort of (key, position) groups the occurrences of each
 //      pair; per distinct pair, its count is a difference of a prefix sum;
 //   3. candidates (count >= 2) ranked by (count desc, key asc) with a second
@@ -48,28 +51,36 @@ __global__ void k_eq_run_marks(const int32_t* __restrict__ s, int64_t n, uint32_
     GRID_STRIDE(i, n) mark[i] = (i == 0 || s[i] != s[i - 1]) ? (uint32_t)i : 0u;
 }
 
-// Key of the pair at every position (invalid: all ones), its position, and
-// whether it is a counted (non-overlapping) occurrence.
+// Key of the pair at every position, whether it is a counted
+// (non-overlapping) occurrence, and whether it can reach a count of two this
+// round (rel).  After the first round a pair can only do so when it holds a
+// symbol made by the previous round (>= fresh) or was a candidate then
+// (cand): occurrences of an older pair only ever disappear.
 __global__ void k_pair_keys(const int32_t* __restrict__ s, int64_t n, const uint32_t* __restrict__ eq_start, int b,
-                            uint64_t invalid, uint64_t* key, uint32_t* pos, uint8_t* counted,
-                            unsigned long long* n_valid) {
-    unsigned long long nv = 0;
+                            int32_t fresh, const uint8_t* __restrict__ cand, uint64_t* key, uint8_t* counted,
+                            uint32_t* rel) {
     GRID_STRIDE(i, n) {
-        bool valid = false, cnt = false;
+        bool valid = false, cnt = false, r = false;
         if (i + 1 < n) {
             const int32_t x = s[i], y = s[i + 1];
             valid = x != 0 && y != 0;
             cnt = valid && (x != y || ((i - (int64_t)eq_start[i]) & 1) == 0);
-            key[i] = valid ? (((uint64_t)(uint32_t)x << b) | (uint32_t)y) : invalid;
-        } else {
-            key[i] = invalid;
+            r = valid && (cand == nullptr || x >= fresh || y >= fresh || cand[i]);
+            key[i] = ((uint64_t)(uint32_t)x << b) | (uint32_t)y;
         }
-        pos[i] = (uint32_t)i;
         counted[i] = cnt;
-        nv += valid;
+        rel[i] = r;
     }
-    for (int o = 16; o; o >>= 1) nv += __shfl_xor_sync(0xffffffffu, nv, o);
-    if ((threadIdx.x & 31) == 0 && nv) atomicAdd(n_valid, nv);
+}
+
+// The relevant pairs, compacted (keys and positions) in position order.
+__global__ void k_pick_pairs(const uint64_t* __restrict__ key, const uint32_t* __restrict__ rel,
+                             const uint32_t* __restrict__ rpos, int64_t n, uint64_t* ko, uint32_t* po) {
+    GRID_STRIDE(i, n) {
+        if (!rel[i]) continue;
+        ko[rpos[i]] = key[i];
+        po[rpos[i]] = (uint32_t)i;
+    }
 }
 
 // Over the sorted occurrences [0, nv): start of each distinct pair, and the
@@ -190,10 +201,15 @@ __global__ void k_rewrite(const int32_t* __restrict__ s, int64_t n, const uint8_
     }
 }
 
+// Compaction of the rewritten string; the candidate flag of each surviving
+// position goes along (for the next round's relevant pairs).
 __global__ void k_compact(const int32_t* __restrict__ sym, const uint32_t* __restrict__ keep,
-                          const uint32_t* __restrict__ kpre, int64_t n, int32_t* out) {
+                          const uint32_t* __restrict__ kpre, const uint32_t* __restrict__ rank_pos, int64_t n,
+                          int32_t* out, uint8_t* cand_out) {
     GRID_STRIDE(i, n) {
-        if (keep[i]) out[kpre[i]] = sym[i];
+        if (!keep[i]) continue;
+        out[kpre[i]] = sym[i];
+        cand_out[kpre[i]] = rank_pos[i] != NONE;
     }
 }
 
@@ -245,7 +261,8 @@ extern "C" int gmr_repair_compress_device(const gmr_csrv* m, int device, gmr_gra
         if (n) GMR_CUDA(cudaMemcpyAsync(s.p, m->codes.data(), (size_t)n * 4, cudaMemcpyHostToDevice, st));
         DevArray<uint64_t> ka(cap), kb(cap);
         DevArray<uint32_t> pa(cap), pb(cap), w1(cap + 1), w2(cap + 1), w3(cap + 1);
-        DevArray<uint8_t> counted(cap), chosen(cap), want(cap);
+        DevArray<uint8_t> counted(cap), chosen(cap), want(cap), cand(cap), cand2(cap);
+        int32_t fresh = alpha;  // first symbol made by the previous round
         DevArray<uint32_t> tmp(std::max(dev::sort_scratch(cap), dev::scan_scratch(cap + 1)) + 1);
         DevArray<unsigned long long> cnt(4);
         std::vector<int32_t> rules;           // host copy, appended per round
@@ -256,18 +273,20 @@ extern "C" int gmr_repair_compress_device(const gmr_csrv* m, int device, gmr_gra
             const int64_t maxsym = (int64_t)alpha + (int64_t)rules.size() / 2;
             const int b = bits_of((uint64_t)maxsym + 1);
             if (2 * b > 64) throw Error(GMR_ERR_RANGE, "device RePair: pair keys exceed 64 bits");
-            const uint64_t invalid = 2 * b == 64 ? ~0ull : (1ull << (2 * b)) - 1;
-            // (1) run starts of equal symbols, pair keys, counted occurrences
+            // (1) run starts of equal symbols, pair keys, counted occurrences,
+            // and the pairs that can be candidates, compacted
             LAUNCH(k_eq_run_marks, n, s.p, n, w1.p);
             dev::inclusive_max_scan(w1.p, w1.p, n, tmp.p, st);
             GMR_CUDA(cudaMemsetAsync(cnt.p, 0, 4 * 8, st));
-            LAUNCH(k_pair_keys, n, s.p, n, w1.p, b, invalid, ka.p, pa.p, counted.p, cnt.p);
-            const int64_t nv = (int64_t)read1(cnt.p, st);
+            LAUNCH(k_pair_keys, n, s.p, n, w1.p, b, fresh, round == 0 ? nullptr : cand.p, ka.p, counted.p, w2.p);
+            dev::exclusive_scan(w2.p, w3.p, n, tmp.p, st);
+            const int64_t nv = (int64_t)read1(w3.p + n, st);
             if (nv < 2) break;
+            LAUNCH(k_pick_pairs, n, ka.p, w2.p, w3.p, n, kb.p, pb.p);
             // (2) group occurrences of each pair
-            uint64_t *k1 = ka.p, *k2 = kb.p;
-            uint32_t *p1 = pa.p, *p2 = pb.p;
-            dev::radix_sort(k1, k2, p1, p2, n, 2 * b, tmp.p, st);
+            uint64_t *k1 = kb.p, *k2 = ka.p;
+            uint32_t *p1 = pb.p, *p2 = pa.p;
+            dev::radix_sort(k1, k2, p1, p2, nv, 2 * b, tmp.p, st);
             // w1 = group start flags, w2 = group index (exclusive), w3 = counted prefix
             LAUNCH(k_groups, nv, k1, p1, counted.p, nv, w1.p, w3.p);
             dev::exclusive_scan(w1.p, w2.p, nv, tmp.p, st);
@@ -319,7 +338,9 @@ extern "C" int gmr_repair_compress_device(const gmr_csrv* m, int device, gmr_gra
             LAUNCH(k_rewrite, n, s.p, n, chosen.p, rank_pos, acc.p, apre, (int32_t)maxsym, s2.p, keep);
             dev::exclusive_scan(keep, w2.p, n, tmp.p, st);
             const int64_t n2 = (int64_t)read1(w2.p + n, st);
-            LAUNCH(k_compact, n, s2.p, keep, w2.p, n, s.p);
+            LAUNCH(k_compact, n, s2.p, keep, w2.p, rank_pos, n, s.p, cand2.p);
+            cand.swap(cand2);
+            fresh = (int32_t)maxsym;  // symbols made this round start here
             GMR_CUDA(cudaStreamSynchronize(st));
             if (verbose)
                 std::fprintf(stderr, "device repair round %d: %lld -> %lld symbols, %lld candidates, %zu rules, %.3fs\n",
