@@ -1,8 +1,9 @@
 """ctypes wrapper of the oracle (oracle.c) -- TEST INFRASTRUCTURE ONLY.
 
-Imported by tests/, by the smoke check in __graft_entry__.py and by the CPU
-baseline leg of bench.py, as the checker (and as the timed CPU baseline).  The
-product path (g-mm-repair_gb300/gmr) never imports it.  Each function names the
+Imported by tests/, by the smoke check in __graft_entry__.py, by the CPU
+baseline leg of bench.py and by `bench.py --impl reference`, as the checker
+and as the timed baselines (the reference's CPU sweep, and its GPU engine run
+through RefGpu).  The product path (g-mm-repair_gb300/gmr) never imports it.  Each function names the
 reference code it restates (see oracle.c).
 """
 from __future__ import annotations
