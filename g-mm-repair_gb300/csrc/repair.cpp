@@ -131,12 +131,19 @@ extern "C" int gmr_repair_compress(const gmr_csrv* m, int n_threads, gmr_grammar
         };
 
         std::vector<int32_t> rules;
+        // After the first round only pairs that hold a symbol made by the
+        // previous round (>= fresh) or were candidates in it (was_cand, one flag
+        // per position) can reach a count of two: an older pair's occurrences
+        // only disappear.  Only those are counted.
+        std::vector<uint8_t> was_cand;
+        int32_t fresh = alpha;
         const int P = T;  // shards
         const uint32_t NONE = UINT32_MAX;
         const bool verbose = std::getenv("GMR_VERBOSE") != nullptr;
         for (int round = 0; round < 100000; ++round) {
             auto t_round = std::chrono::steady_clock::now();
             std::vector<int64_t> cs = make_chunks(n);
+            const int32_t round_first = alpha + (int32_t)(rules.size() / 2);  // first symbol made this round
             // (1) count
             std::vector<std::vector<PairMap>> local(T);
             parallel_for_threads(T, [&](int t) {
@@ -158,6 +165,7 @@ extern "C" int gmr_repair_compress(const gmr_csrv* m, int n_threads, gmr_grammar
                     } else {
                         prev_eq_counted = false;
                     }
+                    if (round > 0 && x < fresh && y < fresh && !was_cand[i]) continue;
                     uint64_t k = pkey(x, y);
                     local[t][hkey(k) % P].add(k, 1);
                 }
@@ -248,8 +256,10 @@ extern "C" int gmr_repair_compress(const gmr_csrv* m, int n_threads, gmr_grammar
             bool any = false;
             for (size_t r = 0; r < nc && !any; ++r) any = newsym[r] >= 0;
             if (!any) break;
-            // pass B: same traversal, write accepted replacements in place
+            // pass B: same traversal, write accepted replacements in place; each
+            // written position keeps whether its pair was a candidate
             std::vector<int64_t> outlen(T, 0);
+            std::vector<uint8_t> cnew((size_t)n);
             parallel_for_threads(T, [&](int t) {
                 int64_t a = cs[t], b = cs[t + 1];
                 int64_t i = a, w = a;
@@ -259,14 +269,18 @@ extern "C" int gmr_repair_compress(const gmr_csrv* m, int n_threads, gmr_grammar
                     if (ri != NONE && ri <= rn) {
                         int32_t ns = newsym[ri];
                         if (ns >= 0) {
+                            cnew[w] = 0;
                             s[w++] = ns;
                         } else {
+                            cnew[w] = 1;
                             s[w++] = s[i];
+                            cnew[w] = rn != NONE;
                             s[w++] = s[i + 1];
                         }
                         i += 2;
                         ri = rank_at(i, b);
                     } else {
+                        cnew[w] = ri != NONE;
                         s[w++] = s[i];
                         i += 1;
                         ri = rn;
@@ -278,8 +292,12 @@ extern "C" int gmr_repair_compress(const gmr_csrv* m, int n_threads, gmr_grammar
             int64_t w = outlen[0];
             for (int t = 1; t < T; ++t) {
                 std::memmove(&s[w], &s[cs[t]], (size_t)outlen[t] * sizeof(int32_t));
+                std::memmove(&cnew[w], &cnew[cs[t]], (size_t)outlen[t]);
                 w += outlen[t];
             }
+            cnew.resize((size_t)w);
+            was_cand.swap(cnew);
+            fresh = round_first;
             if (verbose)
                 std::fprintf(stderr, "repair round %d: %lld -> %lld symbols, %zu candidates, %zu rules, %.3fs\n",
                              round, (long long)n, (long long)w, nc, rules.size() / 2,
