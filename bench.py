@@ -279,31 +279,100 @@ def oracle_x(sr: int, Xh: np.ndarray, col: int) -> np.ndarray:
     return x.astype(np.float32)
 
 
-def cpu_reference_rate(g, sr, rows, cols, seconds: float, threads: int, gpu_y0=None, x0=None):
-    """The reference's OpenMP CPU sweep (oracle restatement), on the host cores;
-    also checks the GPU's first column against the oracle."""
+def cpu_reference_rate(g, sr, rows, cols, seconds: float, threads: int, sched=None):
+    """The reference's OpenMP CPU sweep (oracle restatement), timed on the host
+    cores over single vectors for about `seconds`."""
     from oracle import oracle as O
 
     t0 = time.perf_counter()
-    sched = O.RefSchedule(g.alpha, g.rules(), g.C())
+    if sched is None:
+        sched = O.RefSchedule(g.alpha, g.rules(), g.C())
     build_s = time.perf_counter() - t0
     V = g.values().astype(np.float32)
     rng = np.random.default_rng(1)
-    n, spent, check = 0, 0.0, None
+    n, spent = 0, 0.0
     while n < 1 or (spent < seconds and n < 20):
-        x = x0 if (n == 0 and x0 is not None) else rng.uniform(-1, 1, cols).astype(np.float32)
+        if sr == 0:
+            x = rng.uniform(-1, 1, cols).astype(np.float32)
+        else:
+            x = oracle_x(sr, make_inputs(sr, cols, 1 if sr == 2 else 32, 1 + n), 0)
         t = time.perf_counter()
-        y_cpu = sched.cpu_reference(sr, V, x, rows, cols, threads=threads)
+        sched.cpu_reference(sr, V, x, rows, cols, threads=threads)
         spent += time.perf_counter() - t
-        if n == 0 and gpu_y0 is not None and x0 is not None:
-            if sr == 0:
-                y64 = sched.sweep_f64(0, V.astype(np.float64), x0, rows, cols)
-                check = {"rel_err_fp64": float(np.abs(gpu_y0.astype(np.float64) - y64).max() /
-                                                max(np.abs(y64).max(), 1e-30))}
-            else:
-                check = {"mismatches_vs_reference_sweep": int(np.sum(gpu_y0.astype(np.int64) != y_cpu))}
         n += 1
-    return n / spent, n, spent, build_s, check
+    return n / spent, n, spent, build_s
+
+
+def column_words(sr, Yh: np.ndarray, b: int) -> np.ndarray:
+    """Right-hand side b of an engine output [rows][words] as int64 / float64."""
+    if sr == 0:
+        return Yh.view(np.float32)[:, b].astype(np.float64)
+    if sr == 1:
+        return ((Yh.view(np.uint32)[:, b // 32] >> np.uint32(b % 32)) & 1).astype(np.int64)
+    return Yh.view(np.int32)[:, b].astype(np.int64)
+
+
+def check_all_columns(sched, V, sr, Xh, Yh, rows, cols, B, threads):
+    """Every right-hand side of a timed multiply against the oracle, on the
+    host cores (one column per thread; the oracle's C calls release the GIL):
+    (+,x) as relative max-norm against the FP64 sweep (cpu_selftest.cpp:67-102),
+    (OR,AND) and (min,+) bit for bit against the reference's int sweep
+    (gpu_engine_test.cu:49-104).  Runs outside the timed region."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    V32 = np.asarray(V, dtype=np.float32)
+    V64 = V32.astype(np.float64)
+
+    def one(b):
+        x = oracle_x(sr, Xh, b)
+        got = column_words(sr, Yh, b)
+        if sr == 0:
+            ref = sched.sweep_f64(0, V64, x, rows, cols)
+            return float(np.abs(got - ref).max(initial=0.0) / max(np.abs(ref).max(initial=0.0), 1e-30)), 0
+        ref = sched.cpu_reference(sr, V32, x, rows, cols, threads=1).astype(np.int64)
+        return 0.0, int(np.sum(got != ref))
+
+    t = time.perf_counter()
+    with ThreadPoolExecutor(max(1, min(threads, B))) as ex:
+        res = list(ex.map(one, range(B)))
+    out = {"columns": B, "seconds": round(time.perf_counter() - t, 1), "threads": max(1, min(threads, B))}
+    if sr == 0:
+        errs = [r[0] for r in res]
+        out |= {"rel_err_fp64_max": max(errs), "worst_column": int(np.argmax(errs)), "tolerance": 1e-5,
+                "ok": bool(max(errs) <= 1e-5)}
+    else:
+        mism = [r[1] for r in res]
+        out |= {"mismatches": int(sum(mism)), "worst_column": int(np.argmax(mism)), "ok": sum(mism) == 0,
+                "against": "the reference's int sweep (oracle restatement), bit for bit"}
+    return out
+
+
+def source_hash() -> str:
+    """Hash of the sources that make the sweep kernels: a traffic figure is
+    only reported for the build it was measured on."""
+    import hashlib
+
+    h = hashlib.sha256()
+    for f in ("g-mm-repair_gb300/csrc/engine.cu", "g-mm-repair_gb300/csrc/device_util.cuh",
+              "g-mm-repair_gb300/csrc/gmr_internal.h", "include/gmr.h"):
+        h.update((REPO / f).read_bytes())
+    return h.hexdigest()[:16]
+
+
+def traffic_entry(key: str):
+    """DRAM bytes per multiply from profiles/traffic.json, or (None, why)."""
+    tf = REPO / "profiles" / "traffic.json"
+    if not tf.exists():
+        return None, "no traffic capture committed"
+    try:
+        ent = json.loads(tf.read_text()).get(key)
+    except Exception as e:  # noqa: BLE001
+        return None, f"unreadable traffic file: {e}"
+    if not isinstance(ent, dict):
+        return None, f"no capture for {key}"
+    if ent.get("source_hash") != source_hash():
+        return None, f"capture {ent.get('source_hash')} is of other kernel sources than this build ({source_hash()})"
+    return ent, None
 
 
 def reference_gpu_rate(g, sr, rows, cols, Xh, B, device, seconds=1.5):
@@ -355,6 +424,16 @@ def workload_config(args, rows, cols):
     return cfg
 
 
+VARIANT_NAMES = {0: "auto (learned per-launch table, CUDA graph)", 1: "plain", 2: "fused", 3: "graph",
+                 4: "persistent"}
+
+
+def run_config(args, rows, cols, ws):
+    """The line's config: the same keys on both arms."""
+    return workload_config(args, rows, cols) | {"variant": VARIANT_NAMES[args.variant],
+                                                "parallelism": f"replicas x{ws}"}
+
+
 def run_reference(args):
     """The reference's CPU implementation of the path on the host cores: one
     step = one vector through the OpenMP layered sweep (gpu_engine_test.cu:49-104,
@@ -385,7 +464,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": v, "unit": "vectors/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * sum(timed) / len(timed),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype_of(sr),
-        "data": "synthetic", "config": workload_config(args, rows, cols),
+        "data": "synthetic", "config": run_config(args, rows, cols, ws),
         "cpu_baseline": {"value": v, "unit": "vectors/s", "cores": threads, "kind": "port",
                          "sample": f"{len(timed)} single vectors of the same grammar, one per step, through the "
                                    f"reference's OpenMP layered CPU sweep (restated in oracle/), {threads} threads; "
@@ -468,14 +547,17 @@ def run_pack8(args):
     import gmr
 
     rng = np.random.default_rng(17)
-    engines, Xs, Ys, Bs, total_alg, info = [], [], [], [], 0.0, []
+    engines, Xs, Ys, Bs, total_alg, info, grammars, Xhs = [], [], [], [], 0.0, [], [], []
     for i in range(8):
         rows, cols = int(rng.integers(5_000, 200_001)), int(rng.integers(1_000, 10_001))
         g, gi = mosaic_grammar(rows, cols, 64, 0.01, 1e-3, 10 + i)
         plan = gmr.Plan.build(g, rows, cols)
         B = [1, 4, 16, 64][i % 4]
         eng = gmr.Engine(plan)
-        X = torch.from_numpy(make_inputs(0, cols, B, 100 + i)).cuda()
+        Xh = make_inputs(0, cols, B, 100 + i)
+        X = torch.from_numpy(Xh).cuda()
+        grammars.append((g, rows, cols))
+        Xhs.append(Xh)
         Y = torch.empty((rows, B), device="cuda")
         st = torch.cuda.current_stream().cuda_stream
         eng.autotune(0, X.data_ptr(), Y.data_ptr(), B, stream=st)
@@ -506,6 +588,16 @@ def run_pack8(args):
     ms = timed_loop(torch, stream, packed, args.steps)
     clocks = sampler.stop()
     vecs = sum(Bs)
+    check = None
+    if not args.no_check:
+        from oracle import oracle as O
+        check = []
+        for (g, rows, cols), Xh, Yd, B in zip(grammars, Xhs, Ys, Bs):
+            sched = O.RefSchedule(g.alpha, g.rules(), g.C())
+            check.append(check_all_columns(sched, g.values(), 0, Xh, Yd.cpu().numpy(), rows, cols, B,
+                                           os.cpu_count() or 1))
+        check = {"grammars": check, "ok": all(c["ok"] for c in check),
+                 "rel_err_fp64_max": max(c["rel_err_fp64_max"] for c in check)}
     out = {"metric": METRIC, "value": vecs * 1000.0 / ms, "unit": "vectors/s", "n_gpus": 1, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -513,7 +605,7 @@ def run_pack8(args):
                       "l2": "inputs larger than L2; no flush"},
            "sequential_vps": vecs * 1000.0 / ms_seq, "pack_gain": ms_seq / ms,
            "step_alg_gbs": total_alg / (ms / 1000.0) / 1e9, "gpu_launches": int(pack.last_launches * args.steps),
-           "clocks": clocks}
+           "clocks": clocks, "check": check}
     print(json.dumps(out), flush=True)
     return 0
 
@@ -604,6 +696,10 @@ def main():
     ap.add_argument("--variant", type=int, default=0,
                     help="0 auto (learned / autotuned per-launch table, CUDA graph), 1 plain, 2 fused, 3 graph, "
                          "4 persistent")
+    ap.add_argument("--push", type=int, default=0, choices=[0, 1, 2],
+                    help="0 the per-launch table decides which levels push their emissions, 1 no level, "
+                         "2 every level")
+    ap.add_argument("--no-check", action="store_true", help="skip checking every column against the oracle")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner and the learned choice")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -673,7 +769,7 @@ def main():
     Y = torch.empty((rows, words), dtype=torch.int32, device=dev)
     stream = torch.cuda.current_stream(dev)
     sp = stream.cuda_stream
-    cfg = dict(variant=args.variant)
+    cfg = dict(variant=args.variant, push=args.push)
 
     def step():
         eng.multiply_device(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, **cfg)
@@ -709,6 +805,8 @@ def main():
     tuning = {}
     if args.variant == 0:
         tuning["default_vps"] = B * 1000.0 / timed(20, variant=3)
+        tuning["default_pull_vps"] = B * 1000.0 / timed(20, variant=3, push=1)
+        tuning["default_push_vps"] = B * 1000.0 / timed(20, variant=3, push=2)
         if not args.no_tune:
             t0 = time.perf_counter()
             eng.autotune(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, reps=3)
@@ -757,6 +855,7 @@ def main():
     if ws > 1:
         torch.distributed.barrier()
     clocks = sampler.stop()
+    Y_timed = Y.cpu().numpy()  # the timed multiplies' result, checked against the oracle below
     ms = slowest_rank_ms(e0.elapsed_time(e1), ws, dev)
     ms_per_step = ms / args.steps
     value = whole_job_vps(ws, B, args.steps, ms)
@@ -779,9 +878,14 @@ def main():
 
     # ---- per-launch times (the same kernels launched one by one) for the roofline
     reps = 5
-    lt = np.mean([eng.time_launches(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, variant=args.variant)
+    lt = np.mean([eng.time_launches(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, **cfg)
                   for _ in range(reps)], axis=0)
-    level_ms = float(lt[1:].sum()) if len(lt) > 1 else float(lt.sum())  # k_level launches (persistent: one)
+    eager_level_ms = float(lt[1:].sum()) if len(lt) > 1 else float(lt.sum())  # k_level launches (persistent: one)
+    # the dominant kernel's time inside the timed graph replay: the step's time
+    # times the level launches' share of the same launches timed one by one
+    level_share = eager_level_ms / float(lt.sum()) if len(lt) > 1 else 1.0
+    level_ms = ms_per_step * level_share
+    assert level_ms <= ms_per_step
     if args.dump_launches:
         ops, ems = plan.level_ops(), plan.level_emits()
         log("launch\tms\tops(level k)\temits(level k-1)")
@@ -803,13 +907,9 @@ def main():
     l2_seq = gmr.measure_gather_bandwidth(64 << 20, device=local, sequential=True)
     value_gbs = vbytes / (level_ms / 1000.0) / 1e9
     step_gbs = alg_total / (ms_per_step / 1000.0) / 1e9
-    traffic = None
-    tf = REPO / "profiles" / "traffic.json"
-    if tf.exists():
-        try:
-            traffic = json.loads(tf.read_text()).get(f"{args.workload}/{args.semiring}/B{B}")
-        except Exception:
-            traffic = None
+    tkey = f"{args.workload}/{args.semiring}/B{B}/push{args.push}"
+    traffic_ent, traffic_why = traffic_entry(tkey)
+    traffic = traffic_ent["dram_bytes_per_multiply"] if traffic_ent else None
 
     # ---- plain per-level sweep, one vector at a time (the reference's scheme)
     x1 = torch.from_numpy(make_inputs(sr, cols, 1, 7).view(np.int32)).to(dev)
@@ -848,14 +948,16 @@ def main():
         "metric": METRIC, "value": value, "unit": "vectors/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": dtype_of(sr), "data": "synthetic (seeded generator + RePair)",
-        "config": workload_config(args, rows, cols) | {
-            "variant": {0: "auto (learned per-launch table, CUDA graph)", 1: "plain", 2: "fused", 3: "graph",
-                        4: "persistent"}[args.variant], "parallelism": f"replicas x{ws}"},
+        "config": run_config(args, rows, cols, ws),
         "tuning": tuning,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "traffic_source": traffic_ent if traffic_ent else {"unavailable": traffic_why},
                      "kernel": "k_level (all level launches of one multiply)",
                      "alg_bytes_per_multiply": alg_level, "kernel_ms_per_multiply": level_ms,
+                     "kernel_ms_source": "timed graph replay (ms_per_step) x the level launches' share of the "
+                                         "same launches timed one by one",
+                     "level_share": level_share, "eager_level_ms": eager_level_ms,
                      "step_alg_gbs": step_gbs,
                      "gather_ceiling": {"value_bytes_per_multiply": vbytes, "achieved_gbs": value_gbs,
                                         "l2_random_128B_gbs": ceil_l2, "hbm_random_128B_gbs": ceil_hbm,
@@ -880,21 +982,17 @@ def main():
         out["cusparse_csr"] = cusparse_baseline(torch, args, rows, cols, B)
         if out["cusparse_csr"] and "spmm_vps" in out["cusparse_csr"]:
             out["cusparse_csr"]["engine_speedup"] = value / out["cusparse_csr"]["spmm_vps"]
+    sched = None
+    threads = os.cpu_count() or 1
+    if rank == 0 and not args.no_check:
+        from oracle import oracle as O
+        sched = O.RefSchedule(g.alpha, g.rules(), g.C())
+        out["check"] = check_all_columns(sched, g.values(), sr, Xh, Y_timed, rows, cols, B, threads)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        yh = Y.cpu().numpy()
-        if sr == 0:
-            y0 = yh.view(np.float32)[:, 0]
-        elif sr == 1:
-            y0 = (yh.view(np.uint32)[:, 0] & np.uint32(1)).astype(np.int64)
-        else:
-            y0 = yh[:, 0]
-        threads = os.cpu_count() or 1
-        rate, n, spent, build_s, check = cpu_reference_rate(g, sr, rows, cols, args.cpu_seconds, threads,
-                                                            gpu_y0=y0, x0=oracle_x(sr, Xh, 0))
+        rate, n, spent, build_s = cpu_reference_rate(g, sr, rows, cols, args.cpu_seconds, threads, sched=sched)
         out["cpu_baseline"] = {"value": rate, "unit": "vectors/s", "cores": threads, "kind": "port",
                                "sample": f"{n} single vectors of the same grammar in {spent:.1f} s with the "
                                          f"reference's OpenMP level sweep (restated in oracle/)"}
-        out["check"] = check
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:

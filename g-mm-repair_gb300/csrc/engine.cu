@@ -200,6 +200,12 @@ struct LevelArgs {
     int em_chunk;       // emissions per lane group (chunked segmented mode)
     bool direct;        // em_src holds terminal codes (see SweepArgs::em_tcode)
     bool direct_ops;    // ops' terminal children are codes: -1 zero terminal, -(code + 2)
+    // Push: the ops of this launch fold their own values into the rows that
+    // emit them (rows of slot s: pe_row[pe_off[s] .. pe_off[s+1])), straight
+    // from registers with one vector reduction per (emission, lane); the next
+    // launch then folds nothing of this level.  nullptr: pulled as usual.
+    const int32_t* pe_off = nullptr;
+    const int32_t* pe_row = nullptr;
 };
 
 template <int GLOG>
@@ -321,7 +327,28 @@ __global__ void __launch_bounds__(256) k_prologue(SweepArgs a) {
                               (int64_t)gridDim.x * blockDim.x);
 }
 
-// Evaluate the ops of one level, two items per thread in flight.
+// Push of two freshly computed values into the rows that emit them: the
+// reductions are fire-and-forget (no value comes back), and Y is small
+// enough to stay in L2, so they cost L2 atomic bandwidth but no gather.
+// Row lists are walked four ahead; the second value's list follows the first.
+template <class S, int VEC>
+__device__ __forceinline__ void push_rows(const SweepArgs& a, const LevelArgs& L, int64_t slot, int tile, int lane,
+                                          const Vec<typename S::T, VEC>& v) {
+    using T = typename S::T;
+    const int32_t p1 = __ldg(L.pe_off + slot + 1);
+    int32_t p = __ldg(L.pe_off + slot);
+    for (; p + 4 <= p1; p += 4) {
+        int32_t r[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) r[j] = __ldg(L.pe_row + p + j);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) vred<S, VEC>(yptr<T>(a, r[j], tile, lane, VEC), v);
+    }
+    for (; p < p1; ++p) vred<S, VEC>(yptr<T>(a, __ldg(L.pe_row + p), tile, lane, VEC), v);
+}
+
+// Evaluate the ops of one level, two items per thread in flight; with
+// L.pe_off set, each value is also pushed into its emitting rows of Y.
 template <class S, int VEC, int GLOG, bool CG = false, bool DIR = false>
 __device__ __forceinline__ void do_ops(const SweepArgs& a, const LevelArgs& L, int tile, int64_t t0,
                                        int64_t stride) {
@@ -345,8 +372,13 @@ __device__ __forceinline__ void do_ops(const SweepArgs& a, const LevelArgs& L, i
                 lb_v.v[j] = S::apply(lb_v.v[j], cb);
             }
         }
-        vstore<T, VEC>(out + sa * a.Bt + la * VEC, voplus<S, VEC>(la_v, ra_v));
-        if (hb) vstore<T, VEC>(out + sb * a.Bt + lb * VEC, voplus<S, VEC>(lb_v, rb_v));
+        const Vec<T, VEC> va = voplus<S, VEC>(la_v, ra_v), vb = voplus<S, VEC>(lb_v, rb_v);
+        vstore<T, VEC>(out + sa * a.Bt + la * VEC, va);
+        if (hb) vstore<T, VEC>(out + sb * a.Bt + lb * VEC, vb);
+        if (L.pe_off) {
+            push_rows<S, VEC>(a, L, sa, tile, la, va);
+            if (hb) push_rows<S, VEC>(a, L, sb, tile, lb, vb);
+        }
     }
 }
 
@@ -623,11 +655,13 @@ static constexpr int64_t kChunkSlots = 1 << 19;  // source slots per chunk (64 M
 struct Launch {
     int semiring, B, Bw, VEC, G, variant, emit, chunk;
     int Bt, ntile, tile_levels;
+    int push_mode;  // GMR_PUSH_*
     unsigned long long spin_limit;
     std::vector<uint8_t> lv;  // per-launch variant (index = launch slot), empty = uniform emit/chunk
     bool operator==(const Launch& o) const {
         return semiring == o.semiring && B == o.B && Bw == o.Bw && VEC == o.VEC && variant == o.variant &&
-               emit == o.emit && chunk == o.chunk && Bt == o.Bt && tile_levels == o.tile_levels && lv == o.lv;
+               emit == o.emit && chunk == o.chunk && Bt == o.Bt && tile_levels == o.tile_levels &&
+               push_mode == o.push_mode && lv == o.lv;
     }
 };
 
@@ -667,6 +701,11 @@ struct gmr_engine {
     gmr::DevBuf em_tcode, rule_terms, ops_direct;
     int64_t n_rule_terms = 0;
     bool direct_terms = false;
+    // Push lists (LevelArgs::pe_off): the emissions of levels 1..depth ordered
+    // by source slot, rows ascending per slot; push_ok[k] = every emission of
+    // level k has a slot of level k as its source, so level k can push.
+    gmr::DevBuf pe_off, pe_row;
+    std::vector<uint8_t> push_ok;
     // Left product (y = x^T M): flat edge lists uploaded by gmr_engine_enable_left.
     gmr::DevBuf le_src, le_tgt, le_split, tcol_off, tcol_q;
     std::vector<int64_t> le_off;
@@ -683,7 +722,8 @@ struct gmr_engine {
     std::vector<gmr::DevBuf*> schedule_bufs() {
         return {&ops, &op_c, &em_src, &em_row, &seg_row, &seg_start, &term_val, &term_col, &V,
                 &d_lvl_off, &d_em_off, &d_seg_off, &sync, &em_src_c, &em_row_c, &seg_row_c, &seg_start_c,
-                &le_src, &le_tgt, &le_split, &tcol_off, &tcol_q, &em_tcode, &rule_terms, &ops_direct};
+                &le_src, &le_tgt, &le_split, &tcol_off, &tcol_q, &em_tcode, &rule_terms, &ops_direct,
+                &pe_off, &pe_row};
     }
 };
 
@@ -691,6 +731,16 @@ namespace gmr {
 
 
 static int words_per_slot(int semiring, int B) { return semiring == GMR_BOOLEAN ? (B + 31) / 32 : B; }
+
+// Whether the rules of level k push their own emissions in this multiply.
+static bool push_level(const gmr_engine* e, const Launch& lc, int k) {
+    if (lc.variant == GMR_VARIANT_PLAIN || lc.variant == GMR_VARIANT_PERSISTENT) return false;
+    if (k < 1 || k > e->depth || k >= (int)e->push_ok.size() || !e->push_ok[k]) return false;
+    if (lc.push_mode == GMR_PUSH_NEVER) return false;
+    if (lc.push_mode == GMR_PUSH_ALWAYS) return true;
+    if (!lc.lv.empty() && k < (int)lc.lv.size()) return (lc.lv[k] & GMR_LEVEL_PUSH) != 0;
+    return false;
+}
 
 // Optional per-launch timing: an event is recorded before the first launch
 // and after every launch.
@@ -782,13 +832,20 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
         int emit = lc.emit, chunk = lc.chunk, ops_cap = kOpsCtasPerSm[0];
         bool by_chunk = false;
         if (!lc.lv.empty() && slot < (int)lc.lv.size()) {
-            const int v = lc.lv[slot] % GMR_N_LEVEL_VARIANTS;
+            const int v = (lc.lv[slot] & ~GMR_LEVEL_PUSH) % GMR_N_LEVEL_VARIANTS;
             emit = kEmitVariants[v % kNumEmitVariants].emit;
             chunk = kEmitVariants[v % kNumEmitVariants].chunk;
             ops_cap = kOpsCtasPerSm[(v / kNumEmitVariants) % 2];
             by_chunk = v >= 2 * kNumEmitVariants;
         }
         if (lc.variant == GMR_VARIANT_PLAIN) emit = GMR_EMIT_ATOMIC;
+        // level k_em pushed its emissions in its own launch: nothing to fold
+        if (k_em >= 1 && push_level(e, lc, k_em)) k_em = -1;
+        if (k_ops >= 1 && push_level(e, lc, k_ops)) {
+            L.pe_off = static_cast<const int32_t*>(e->pe_off.p);
+            L.pe_row = static_cast<const int32_t*>(e->pe_row.p);
+            if (emit == GMR_EMIT_ROWS) emit = GMR_EMIT_SEGMENTED;  // the pushes are atomics into the same Y
+        }
         if (k_em == 0 && e->direct_terms) {  // terminal emissions fold leaf(V, X) directly
             L.em_src = static_cast<const int32_t*>(e->em_tcode.p);
             L.direct = true;
@@ -1013,6 +1070,8 @@ static Launch resolve_launch(gmr_engine* e, int semiring, int B, const void* X, 
     }
     lc.emit = cfg && cfg->emit_mode ? cfg->emit_mode : GMR_EMIT_SEGMENTED;
     if (lc.variant == GMR_VARIANT_PLAIN) lc.emit = GMR_EMIT_ATOMIC;
+    lc.push_mode = cfg ? cfg->push : GMR_PUSH_AUTO;
+    if (lc.push_mode < GMR_PUSH_AUTO || lc.push_mode > GMR_PUSH_ALWAYS) throw Error(GMR_ERR_ARG, "unknown push mode");
     lc.chunk = cfg && cfg->ops_per_cta > 0 ? cfg->ops_per_cta : 16;
     int bt = cfg && cfg->vec_tile > 0 ? cfg->vec_tile : auto_tile(e, lc.Bw);
     if (bt > lc.Bw || lc.Bw % bt != 0) bt = lc.Bw;  // tiles must divide the batch
@@ -1221,6 +1280,35 @@ static void build_direct_terms(const gmr_plan& p, gmr_engine& e) {
     upload(list, e.rule_terms);
 }
 
+// Push lists (gmr_engine::pe_*): a counting sort of the emissions of levels
+// 1..depth by source slot.  The plan orders a level's emissions by (row,
+// source), so each slot's rows come out ascending.  Offsets are int32: a
+// plan with 2^31 or more such emissions gets no push lists.
+static void build_push_lists(const gmr_plan& p, gmr_engine& e) {
+    const int D = p.depth;
+    e.push_ok.assign(D + 2, 0);
+    if (D < 1) return;
+    const int64_t E0 = p.em_off[1], E1 = p.em_off[D + 1];
+    if (E1 - E0 >= (int64_t)INT32_MAX || p.n_ops() >= (int64_t)INT32_MAX) return;
+    std::vector<int32_t> off((size_t)p.n_ops() + 1, 0);
+    for (int k = 1; k <= D; ++k) {
+        bool ok = true;
+        for (int64_t j = p.em_off[k]; j < p.em_off[k + 1] && ok; ++j)
+            ok = p.em_src[j] >= p.lvl_off[k - 1] && p.em_src[j] < p.lvl_off[k];
+        e.push_ok[k] = ok;
+        if (!ok) continue;
+        for (int64_t j = p.em_off[k]; j < p.em_off[k + 1]; ++j) off[(size_t)p.em_src[j] + 1]++;
+    }
+    for (size_t s = 0; s + 1 < off.size(); ++s) off[s + 1] += off[s];
+    std::vector<int32_t> row((size_t)std::max<int32_t>(off.back(), 1)), fill(off.begin(), off.end() - 1);
+    for (int k = 1; k <= D; ++k) {
+        if (!e.push_ok[k]) continue;
+        for (int64_t j = p.em_off[k]; j < p.em_off[k + 1]; ++j) row[(size_t)fill[(size_t)p.em_src[j]]++] = p.em_row[j];
+    }
+    upload(off, e.pe_off);
+    upload(row, e.pe_row);
+}
+
 extern "C" int gmr_engine_create(const gmr_plan* p, int device, gmr_engine** out) {
     return guarded([&] {
         if (!p || !out) throw Error(GMR_ERR_ARG, "null argument");
@@ -1261,6 +1349,7 @@ extern "C" int gmr_engine_create(const gmr_plan* p, int device, gmr_engine** out
             upload(p->term_col, e->term_col);
             upload(p->V, e->V);
             build_direct_terms(*p, *e);
+            build_push_lists(*p, *e);
             GMR_CUDA(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking));
             GMR_CUDA(cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, device));
         } catch (...) {
@@ -1389,7 +1478,7 @@ extern "C" int gmr_engine_set_level_variants(gmr_engine* e, int semiring, int B,
         }
         if (n != e->depth + 2) throw Error(GMR_ERR_ARG, "need depth + 2 = " + std::to_string(e->depth + 2) + " entries");
         for (int i = 0; i < n; ++i)
-            if (v[i] >= GMR_N_LEVEL_VARIANTS) throw Error(GMR_ERR_ARG, "variant index out of range");
+            if ((v[i] & ~GMR_LEVEL_PUSH) >= GMR_N_LEVEL_VARIANTS) throw Error(GMR_ERR_ARG, "variant index out of range");
         e->level_variants[{semiring, B}] = std::vector<uint8_t>(v, v + n);
     });
 }
@@ -1465,6 +1554,54 @@ extern "C" int gmr_engine_autotune_energy(gmr_engine* e, int semiring, const voi
             if (tolerance > 0.0f && b < 10 && med[(size_t)l * nv + twin] <= med[(size_t)l * nv + b] * (1.0f + tolerance))
                 b = twin;
             best[l] = (uint8_t)b;
+        }
+        // Push or pull, per level.  Slot k costs o_k (rules of level k) +
+        // p_k (if level k pushes) + f_{k-1} (if level k-1 does not push).
+        // Four tables measure it: none pushing (o_k + f_{k-1}), all pushing
+        // (o_k + p_k), odd levels pushing and even levels pushing (o_k alone in
+        // every slot whose level pushes nothing while the level below does).
+        // Level k pushes when p_k < f_k.  A level whose emissions cannot be
+        // pushed is never flagged, and the formulas stay exact around it.
+        const int D = e->depth;
+        bool can_push = false;
+        for (int k = 1; k <= D && k < (int)e->push_ok.size(); ++k) can_push |= e->push_ok[k] != 0;
+        if (can_push && D >= 1) {
+            auto slot_times = [&](const std::vector<uint8_t>& table) {
+                if (gmr_engine_set_level_variants(e, semiring, B, table.data(), nl) != GMR_OK)
+                    throw Error(GMR_ERR_ARG, gmr_last_error());
+                std::vector<std::vector<float>> runs;
+                for (int r = 0; r < reps; ++r) {
+                    int n = 0;
+                    gmr_config c{};
+                    int rc = gmr_engine_time_launches(e, semiring, dX, dY, B, &c, stream, buf.data(), (int)buf.size(), &n);
+                    if (rc != GMR_OK) throw Error(rc, gmr_last_error());
+                    if (n != nl) throw Error(GMR_ERR_STATE, "unexpected launch count " + std::to_string(n));
+                    runs.emplace_back(buf.begin(), buf.begin() + n);
+                }
+                std::vector<float> out(nl);
+                for (int l = 0; l < nl; ++l) {
+                    std::vector<float> xs;
+                    for (auto& r : runs) xs.push_back(r[l]);
+                    std::nth_element(xs.begin(), xs.begin() + xs.size() / 2, xs.end());
+                    out[l] = xs[xs.size() / 2];
+                }
+                return out;
+            };
+            auto with_push = [&](int parity) {  // -1: every level; 0 / 1: even / odd levels
+                std::vector<uint8_t> t = best;
+                for (int k = 1; k <= D; ++k)
+                    if (parity < 0 || (k & 1) == parity) t[k] |= GMR_LEVEL_PUSH;
+                return t;
+            };
+            const std::vector<float> t0 = slot_times(best), t1 = slot_times(with_push(-1));
+            const std::vector<float> todd = slot_times(with_push(1)), teven = slot_times(with_push(0));
+            auto ops_only = [&](int k) { return (k & 1) ? teven[k] : todd[k]; };
+            for (int k = 1; k <= D; ++k) {
+                if (k >= (int)e->push_ok.size() || !e->push_ok[k]) continue;
+                const float pk = t1[k] - ops_only(k);
+                const float fk = k < D ? t0[k + 1] - ops_only(k + 1) : t0[D + 1];
+                if (pk < fk) best[k] |= GMR_LEVEL_PUSH;
+            }
         }
         if (gmr_engine_set_level_variants(e, semiring, B, best.data(), nl) != GMR_OK) throw Error(GMR_ERR_ARG, gmr_last_error());
         if (ms) std::copy(med.begin(), med.end(), ms);
@@ -2090,6 +2227,31 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[GMR_NOALLOC_SCR
 static void* g_noalloc_addr[64] = {};
 static std::mutex g_noalloc_mu;
 
+// Every kernel the entry point can launch, for one semiring.  Querying a
+// kernel's attributes loads its code onto the current device, so the set-up
+// call below leaves nothing for a later call's first launch to load.
+template <class S, int VEC, int GLOG>
+static void noalloc_touch_one() {
+    cudaFuncAttributes fa;
+    GMR_CUDA(cudaFuncGetAttributes(&fa, k_prologue<S, VEC, GLOG>));
+    GMR_CUDA(cudaFuncGetAttributes(&fa, k_level<S, VEC, GLOG, GMR_EMIT_ROWS>));
+}
+template <class S>
+static void noalloc_touch() {
+    noalloc_touch_one<S, 4, 0>();
+    noalloc_touch_one<S, 4, 1>();
+    noalloc_touch_one<S, 4, 2>();
+    noalloc_touch_one<S, 4, 3>();
+    noalloc_touch_one<S, 4, 4>();
+    noalloc_touch_one<S, 4, 5>();
+    noalloc_touch_one<S, 4, -1>();
+    noalloc_touch_one<S, 2, 0>();
+    noalloc_touch_one<S, 1, 0>();
+    noalloc_touch_one<S, 1, -1>();
+}
+
+// Set-up, once per device with that device current: the array's device
+// address, and the code of every kernel the entry point launches.
 static void* noalloc_scratch_for_current_device() {
     int dev = -1;
     GMR_CUDA(cudaGetDevice(&dev));
@@ -2098,6 +2260,9 @@ static void* noalloc_scratch_for_current_device() {
     if (!g_noalloc_addr[dev]) {
         void* ptr = nullptr;
         GMR_CUDA(cudaGetSymbolAddress(&ptr, g_noalloc_scratch));
+        noalloc_touch<SPlus>();
+        noalloc_touch<SBool>();
+        noalloc_touch<STrop>();
         g_noalloc_addr[dev] = ptr;
     }
     return g_noalloc_addr[dev];
@@ -2190,6 +2355,15 @@ extern "C" int gmr_multiply_noalloc(const gmr_device_plan* p, int semiring, cons
             throw Error(GMR_ERR_ARG, "misaligned device pointer");
         if (p->lvl_off[0] != 0 || p->lvl_off[p->depth] != p->n_ops)
             throw Error(GMR_ERR_FORMAT, "level offsets do not cover the rules");
+        for (int k = 1; k <= p->depth; ++k)
+            if (p->lvl_off[k] < p->lvl_off[k - 1]) throw Error(GMR_ERR_FORMAT, "level offsets decrease");
+        if (p->seg_off[0] != 0) throw Error(GMR_ERR_FORMAT, "row segment offsets do not start at 0");
+        for (int k = 0; k <= p->depth; ++k)
+            if (p->seg_off[k + 1] < p->seg_off[k]) throw Error(GMR_ERR_FORMAT, "row segment offsets decrease");
+        if (p->seg_off[p->depth + 1] > 0 && (!p->em_src || !p->seg_row))
+            throw Error(GMR_ERR_ARG, "null emission array (em_src or seg_row) with emissions present");
+        if ((uintptr_t)p->op_c % 4 != 0 || (uintptr_t)p->em_src % 4 != 0 || (uintptr_t)p->seg_row % 4 != 0)
+            throw Error(GMR_ERR_ARG, "misaligned device pointer");
         const int Bw = words_per_slot(semiring, B);
         const uint64_t arena_bytes = ((uint64_t)p->n_ops * Bw * 4 + 255) / 256 * 256;
         const uint64_t need = arena_bytes + (uint64_t)p->n_terms * Bw * 4;
@@ -2212,7 +2386,7 @@ extern "C" int gmr_multiply_noalloc(const gmr_device_plan* p, int semiring, cons
 }
 
 // ------------------------------------------------------------------ legacy ABI
-// The reference's two entry points (gpu_engine.h:239-276).  Per call: relayout
+// The reference's two entry points (gpu_engine.h:99-136).  Per call: relayout
 // the given proper-layered schedule into a plan, upload, run `iters`
 // multiplies timed with CUDA events, optionally measure energy with NVML,
 // print the reference's stdout lines (gpu_engine.cu:279-280, 337-340, 546-547),

@@ -6,7 +6,7 @@ include/gmr.h).  It mirrors the reference's interface for this path:
 * the file format and loaders of gpu-engine/gpu_engine_test.cu:291-345
   (:class:`Grammar`, ``Grammar.load``);
 * the schedule builder, build_schedule.cpp:42-227 (:class:`Plan`);
-* the engine entry points gpu_engine.h:239-276 (:func:`run_gpu_right_multiply_layered`,
+* the engine entry points gpu_engine.h:99-136 (:func:`run_gpu_right_multiply_layered`,
   :func:`run_gpu_right_multiply_batched`) and the load-once handle API
   (:class:`Engine`).
 
@@ -30,6 +30,8 @@ TROPICAL_INF = 1_000_000_000
 
 VARIANT_AUTO, VARIANT_PLAIN, VARIANT_FUSED, VARIANT_GRAPH, VARIANT_PERSISTENT = 0, 1, 2, 3, 4
 EMIT_AUTO, EMIT_ATOMIC, EMIT_SEGMENTED, EMIT_ROWS = 0, 1, 2, 3
+PUSH_AUTO, PUSH_NEVER, PUSH_ALWAYS = 0, 1, 2
+LEVEL_PUSH = 32
 
 __all__ = [
     "GmrError", "Csrv", "Grammar", "Plan", "Engine", "gen_mosaic", "gen_copy_graph", "repair", "semiring_id",
@@ -419,8 +421,8 @@ class Engine:
         self.close()
 
     @staticmethod
-    def _cfg(variant=0, emit_mode=0, ops_per_cta=0, vec_tile=0, tile_levels=0, spin_limit=0):
-        return Config(variant, vec_tile, ops_per_cta, emit_mode, tile_levels, spin_limit)
+    def _cfg(variant=0, emit_mode=0, ops_per_cta=0, vec_tile=0, tile_levels=0, spin_limit=0, push=0):
+        return Config(variant, vec_tile, ops_per_cta, emit_mode, tile_levels, spin_limit, push)
 
     def status(self):
         """(failed, phase) of the last persistent multiply (after a stream synchronize)."""

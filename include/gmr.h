@@ -5,7 +5,7 @@
  * Two groups of entry points:
  *
  *  1. The drop-in legacy pair, with exactly the signatures of the
- *     reference's gpu-engine/gpu_engine.h:239-276
+ *     reference's gpu-engine/gpu_engine.h:99-136
  *       run_gpu_right_multiply_layered   (replaces gpu_engine.cu:364-397)
  *       run_gpu_right_multiply_batched   (replaces gpu_engine.cu:563-586)
  *     They take the reference's proper-layered schedule (LayeredRule +
@@ -239,7 +239,14 @@ typedef struct {
                          all tiles per launch (0 = by level size) */
     int spin_limit;   /* GMR_VARIANT_PERSISTENT: polls a grid-barrier wait
                          may take before it gives up (0 = 20,000,000) */
+    int push;         /* GMR_PUSH_*: whether rules fold their own values into
+                         the rows that emit them (see GMR_LEVEL_PUSH) */
 } gmr_config;
+enum {
+    GMR_PUSH_AUTO = 0,   /* the installed per-launch table, else the engine's rule */
+    GMR_PUSH_NEVER = 1,  /* every level's emissions are gathered by the next launch */
+    GMR_PUSH_ALWAYS = 2  /* every level that can push does */
+};
 enum {
     GMR_VARIANT_AUTO = 0,
     GMR_VARIANT_PLAIN = 1,   /* per-level launches, one atomic per emission */
@@ -286,8 +293,14 @@ int gmr_engine_time_launches(gmr_engine* e, int semiring, const void* dX, void* 
  * c = 1 folds the emissions one source chunk (2^19 slots of the level) at a
  * time, one launch per chunk, so the chunk's values stay in L2.  An installed
  * table is used by GMR_VARIANT_AUTO multiplies of that (semiring, B).
+ * Adding GMR_LEVEL_PUSH to slot k's entry (1 <= k <= depth) makes the rules of
+ * level k push their values into the rows that emit them as soon as they are
+ * computed (vector reductions into Y, which stays in L2), so launch k+1
+ * gathers nothing of level k; a launch that pushes folds level k-1 with
+ * atomics (a row-owned fold there becomes the segmented one).
  * n = depth + 2; v = NULL clears. */
 #define GMR_N_LEVEL_VARIANTS 20
+#define GMR_LEVEL_PUSH 32
 int gmr_engine_set_level_variants(gmr_engine* e, int semiring, int B, const uint8_t* v, int n);
 int gmr_engine_get_level_variants(const gmr_engine* e, int semiring, int B, uint8_t* v, int cap, int* n);
 /* Exhaustive autotuner: times every variant on every launch (median of
@@ -407,7 +420,7 @@ int64_t gmr_engine_device_bytes(const gmr_engine* e);
 void gmr_engine_free(gmr_engine* e);
 
 /* ------------------------------------------------------------------ */
-/* Drop-in legacy entry points (gpu_engine.h:239-276)                   */
+/* Drop-in legacy entry points (gpu_engine.h:99-136)                   */
 /* ------------------------------------------------------------------ */
 #ifdef __cplusplus
 void run_gpu_right_multiply_layered(
@@ -451,8 +464,13 @@ void run_gpu_right_multiply_batched(
  * the library holds until the process exits.  Larger requests fail with
  * GMR_ERR_RANGE before anything is launched.
  *
- * The first call on a device looks the array up (cudaGetSymbolAddress) with
- * that device current; make that first call before any stream capture.
+ * The first call on a device does the set-up with that device current: it
+ * looks the array up (cudaGetSymbolAddress) and loads the code of every kernel
+ * this entry point can launch (all semirings and widths), so that no later
+ * call loads code onto the device.  Make that first call before any stream
+ * capture and before entering the region that must not allocate.  The address
+ * is kept for the life of the process: resetting the device
+ * (cudaDeviceReset) after the first call is not supported.
  * Every call shares the one array: calls that overlap on the GPU (different
  * streams, or host threads without ordering) race on it and give wrong
  * results; serialize them.  Nothing in the array needs to start at zero:

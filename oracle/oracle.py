@@ -39,12 +39,19 @@ def build(force: bool = False) -> Path:
     return LIB
 
 
+def reference_root() -> Path:
+    """Root of the reference tree: $GMR_REFERENCE, default /root/reference."""
+    return Path(os.environ.get("GMR_REFERENCE", "/root/reference"))
+
+
 def build_ref() -> bool:
     """Builds the reference's own sources into oracle/_ref (only where the
     reference tree exists)."""
-    if not Path("/root/reference/gpu-engine").is_dir():
+    root = reference_root()
+    if not (root / "gpu-engine").is_dir():
         return False
-    r = subprocess.run(["make", "-s", "-C", str(HERE), "ref"], capture_output=True, text=True)
+    r = subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"GMR_REFERENCE={root}"], capture_output=True,
+                       text=True)
     return r.returncode == 0
 
 

@@ -1,9 +1,9 @@
 """Generates the golden fixtures in tests/golden from the REFERENCE's own code.
 
-Run in a container that holds the reference tree (g-mm-repair) at
-/root/reference:
+Run in a container that holds the reference tree (g-mm-repair); its root is
+taken from the environment variable GMR_REFERENCE (default /root/reference):
 
-    python tests/golden/make_golden.py
+    GMR_REFERENCE=/path/to/g-mm-repair python tests/golden/make_golden.py
 
 It builds the reference's sources where they lie (oracle/Makefile -> oracle/_ref:
 cpu_selftest, host_scheduler and ref_tool, a harness that calls the

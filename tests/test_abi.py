@@ -3,6 +3,8 @@ import ctypes
 import re
 from pathlib import Path
 
+import numpy as np
+
 import gmr
 from gmr import _lib
 
@@ -44,3 +46,39 @@ def test_version_and_error_strings():
     h = ctypes.c_void_p()
     rc = lib.gmr_grammar_load(b"/nonexistent/base", ctypes.byref(h))
     assert rc == 3 and b"cannot open" in lib.gmr_last_error()
+
+
+def _bad_device_plan(**over):
+    """A gmr_device_plan that fails the entry point's host-side checks (each
+    case below breaks one), so nothing reaches the GPU."""
+    lvl = np.array([0, 2, 3], dtype=np.int64)
+    seg = np.array([0, 1, 2, 3], dtype=np.int64)
+    dp = _lib.DevicePlan()
+    dp.rows, dp.cols, dp.depth, dp.n_ops, dp.n_terms = 4, 3, 2, 3, 2
+    dp.lvl_off, dp.seg_off = lvl.ctypes.data, seg.ctypes.data
+    dp.ops, dp.em_src, dp.seg_row, dp.seg_start, dp.term_val, dp.term_col, dp.V = [256] * 7
+    dp.op_c = None
+    keep = [lvl, seg]
+    for k, v in over.items():
+        if isinstance(v, np.ndarray):
+            keep.append(v)
+            v = v.ctypes.data
+        setattr(dp, k, v)
+    return dp, keep
+
+
+def test_noalloc_rejects_bad_plans_before_any_launch():
+    lib = gmr.lib()
+    cases = [
+        (dict(em_src=None), 1, b"null emission array"),
+        (dict(seg_row=None), 1, b"null emission array"),
+        (dict(seg_off=np.array([1, 1, 2, 3], dtype=np.int64)), 2, b"do not start at 0"),
+        (dict(seg_off=np.array([0, 2, 1, 3], dtype=np.int64)), 2, b"segment offsets decrease"),
+        (dict(lvl_off=np.array([0, 4, 3], dtype=np.int64)), 2, b"level offsets decrease"),
+        (dict(lvl_off=np.array([0, 2, 5], dtype=np.int64)), 2, b"do not cover"),
+        (dict(op_c=258), 1, b"misaligned"),
+    ]
+    for over, code, msg in cases:
+        dp, keep = _bad_device_plan(**over)
+        rc = lib.gmr_multiply_noalloc(ctypes.byref(dp), 0, ctypes.c_void_p(256), ctypes.c_void_p(256), 4, None)
+        assert rc == code and msg in lib.gmr_last_error(), (over, rc, lib.gmr_last_error())

@@ -101,6 +101,9 @@ CONFIGS = [
     dict(variant=gmr.VARIANT_GRAPH, emit_mode=gmr.EMIT_SEGMENTED, vec_tile=8, ops_per_cta=5),
     dict(variant=gmr.VARIANT_PERSISTENT),                                  # one cooperative launch
     dict(variant=gmr.VARIANT_PERSISTENT, emit_mode=gmr.EMIT_ROWS),
+    dict(variant=gmr.VARIANT_GRAPH, push=gmr.PUSH_ALWAYS),                 # rules push their emissions
+    dict(variant=gmr.VARIANT_FUSED, push=gmr.PUSH_ALWAYS, emit_mode=gmr.EMIT_ROWS, vec_tile=4, tile_levels=2),
+    dict(variant=gmr.VARIANT_FUSED, push=gmr.PUSH_ALWAYS, emit_mode=gmr.EMIT_ATOMIC),
 ]
 
 
@@ -132,10 +135,13 @@ def test_direct_terminal_emissions(case, sr, B, monkeypatch):
     for cfg in CONFIGS:
         check(sr, engine_outputs(sr, eng.multiply(Xw, sr, B=B, **cfg), B), ref)
     rng = np.random.default_rng(B)
-    for table in ([v] * (eng.depth + 2) for v in (0, 3, 4, 10, 13)):
+    for table in ([v] * (eng.depth + 2) for v in (0, 3, 4, 10, 13, 32, 35, 45)):
         eng.set_level_variants(sr, B, table)
         check(sr, engine_outputs(sr, eng.multiply(Xw, sr, B=B), B), ref)
     eng.set_level_variants(sr, B, rng.integers(0, eng.N_LEVEL_VARIANTS, eng.depth + 2))
+    check(sr, engine_outputs(sr, eng.multiply(Xw, sr, B=B), B), ref)
+    eng.set_level_variants(sr, B, rng.integers(0, eng.N_LEVEL_VARIANTS, eng.depth + 2) |
+                           (rng.random(eng.depth + 2) < 0.5) * gmr.LEVEL_PUSH)
     check(sr, engine_outputs(sr, eng.multiply(Xw, sr, B=B), B), ref)
 
 
@@ -217,9 +223,11 @@ def test_autotuned_and_mixed_tables(case, sr):
     times = eng.autotune(sr, dX.data_ptr(), dY.data_ptr(), B)
     assert times.shape == (eng.depth + 2, eng.N_LEVEL_VARIANTS) and np.all(times[1:] > 0)
     best = eng.level_variants(sr, B)
-    assert best is not None and np.array_equal(best[1:], times[1:].argmin(axis=1))
+    assert best is not None and np.array_equal(best[1:] & (255 - gmr.LEVEL_PUSH), times[1:].argmin(axis=1))
+    assert not np.any(best[[0, eng.depth + 1]] & gmr.LEVEL_PUSH)  # only levels 1..depth can push
     rng = np.random.default_rng(sr)
-    for table in (best, rng.integers(0, eng.N_LEVEL_VARIANTS, eng.depth + 2)):
+    mixed = rng.integers(0, eng.N_LEVEL_VARIANTS, eng.depth + 2) | (rng.random(eng.depth + 2) < 0.5) * gmr.LEVEL_PUSH
+    for table in (best, rng.integers(0, eng.N_LEVEL_VARIANTS, eng.depth + 2), mixed):
         eng.set_level_variants(sr, B, table)
         Y = engine_outputs(sr, eng.multiply(Xw, sr, B=B), B)  # AUTO uses the table
         check(sr, Y, ref)
@@ -245,7 +253,7 @@ def test_energy_aware_autotune(case, sr):
     for slot in range(1, eng.depth + 2):
         b = int(times[slot].argmin())
         want = b + 10 if b < 10 and times[slot, b + 10] <= times[slot, b] * (1 + tol) else b
-        assert table[slot] == want
+        assert table[slot] & (255 - gmr.LEVEL_PUSH) == want
     check(sr, engine_outputs(sr, eng.multiply(Xw, sr, B=B), B), ref)
     with pytest.raises(gmr.GmrError):
         eng.autotune(sr, dX.data_ptr(), dY.data_ptr(), B, energy_tolerance=1.5)
@@ -312,7 +320,7 @@ def test_chunked_emission_passes(case, sr, monkeypatch):
     for B in (1, 32):
         X = random_X(sr, cols, B, 300 + B)
         ref = oracle_columns(case["sched"], sr, case["V"], X, rows, cols)
-        for v in (10, 12, 13, 14, 17):  # chunked: segmented 16 / 32, row-owned, atomic; 4 CTAs per SM
+        for v in (10, 12, 13, 14, 17, 42, 45):  # chunked: segmented 16 / 32, row-owned, atomic; 4 CTAs per SM; pushed
             eng.set_level_variants(sr, B, np.full(eng.depth + 2, v, dtype=np.uint8))
             Y = engine_outputs(sr, eng.multiply(engine_inputs(sr, X), sr, B=B), B)
             check(sr, Y, ref)
