@@ -696,9 +696,10 @@ def main():
     ap.add_argument("--variant", type=int, default=0,
                     help="0 auto (learned / autotuned per-launch table, CUDA graph), 1 plain, 2 fused, 3 graph, "
                          "4 persistent")
-    ap.add_argument("--push", type=int, default=0, choices=[0, 1, 2],
-                    help="0 the per-launch table decides which levels push their emissions, 1 no level, "
-                         "2 every level")
+    ap.add_argument("--push", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="how each level's emissions reach Y: 0 as the per-launch table says, 1 gathered by the "
+                         "next launch (pull), 2 pushed by every level that can, 3 every level that can "
+                         "interleaves (source chunks, each folded by the next launch)")
     ap.add_argument("--no-check", action="store_true", help="skip checking every column against the oracle")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner and the learned choice")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)

@@ -25,6 +25,7 @@
 #include <dlfcn.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -696,6 +697,7 @@ struct gmr_engine {
     gmr::DevBuf em_src_c, em_row_c, seg_row_c, seg_start_c;
     std::vector<int64_t> ch_off, ch_em, ch_seg;
     bool chunked = false;
+    int64_t chunk_slots = 1 << 19;  // source slots per chunk
     // Direct terminal emissions (SweepArgs::em_tcode): codes of the terminal
     // emissions and the terminals rules reference.
     gmr::DevBuf em_tcode, rule_terms, ops_direct;
@@ -732,14 +734,38 @@ namespace gmr {
 
 static int words_per_slot(int semiring, int B) { return semiring == GMR_BOOLEAN ? (B + 31) / 32 : B; }
 
-// Whether the rules of level k push their own emissions in this multiply.
-static bool push_level(const gmr_engine* e, const Launch& lc, int k) {
-    if (lc.variant == GMR_VARIANT_PLAIN || lc.variant == GMR_VARIANT_PERSISTENT) return false;
-    if (k < 1 || k > e->depth || k >= (int)e->push_ok.size() || !e->push_ok[k]) return false;
-    if (lc.push_mode == GMR_PUSH_NEVER) return false;
-    if (lc.push_mode == GMR_PUSH_ALWAYS) return true;
-    if (!lc.lv.empty() && k < (int)lc.lv.size()) return (lc.lv[k] & GMR_LEVEL_PUSH) != 0;
-    return false;
+// How the emissions of level k reach Y in this multiply: gathered by the
+// next launch (pull), pushed by the rules that make them (push), or level k
+// evaluated in source chunks with each chunk's emissions gathered by the
+// launch after it (interleave).
+enum { kFoldPull = 0, kFoldPush = 1, kFoldInterleave = 2 };
+
+// Source chunks of level k's rules (gmr_engine::chunk_slots each).
+static int64_t interleave_chunks(const gmr_engine* e, int k) {
+    const int64_t w = e->lvl_off[k] - e->lvl_off[k - 1];
+    return (w + e->chunk_slots - 1) / e->chunk_slots;
+}
+
+static bool can_push(const gmr_engine* e, int k) {
+    return k >= 1 && k <= e->depth && k < (int)e->push_ok.size() && e->push_ok[k];
+}
+// Interleaving needs the chunked emission order and two chunks or more; the
+// levels that run tile by tile (very wide batches) never interleave.
+static bool can_interleave(const gmr_engine* e, const Launch& lc, int k) {
+    if (k < 1 || k > e->depth || !e->chunked || interleave_chunks(e, k) < 2) return false;
+    const int K = lc.ntile > 1 ? std::min(lc.tile_levels, e->depth) : 0;
+    return k > K;
+}
+
+static int level_mode(const gmr_engine* e, const Launch& lc, int k) {
+    if (lc.variant == GMR_VARIANT_PLAIN || lc.variant == GMR_VARIANT_PERSISTENT) return kFoldPull;
+    if (k < 1 || k > e->depth || lc.push_mode == GMR_PUSH_NEVER) return kFoldPull;
+    if (lc.push_mode == GMR_PUSH_ALWAYS) return can_push(e, k) ? kFoldPush : kFoldPull;
+    if (lc.push_mode == GMR_PUSH_INTERLEAVE) return can_interleave(e, lc, k) ? kFoldInterleave : kFoldPull;
+    if (lc.lv.empty() || k >= (int)lc.lv.size()) return kFoldPull;
+    if ((lc.lv[k] & GMR_LEVEL_INTERLEAVE) && can_interleave(e, lc, k)) return kFoldInterleave;
+    if ((lc.lv[k] & GMR_LEVEL_PUSH) && can_push(e, k)) return kFoldPush;
+    return kFoldPull;
 }
 
 // Optional per-launch timing: an event is recorded before the first launch
@@ -816,8 +842,12 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
         k_prologue<S, VEC, GLOG><<<grid, TPB, 0, st>>>(a);
         after();
     }
-    // ops of level k_ops (0: none) and emissions of level k_em (-1: none), tiles [t0, t0+nt)
-    auto level = [&](int k_ops, int k_em, int t0, int nt, bool split) {
+    // ops of level k_ops (0: none) and emissions of level k_em (-1: none), tiles [t0, t0+nt).
+    // ops_lo >= 0: only the ops slots [ops_lo, ops_hi) of level k_ops.  em_part >= 0: fold
+    // only that source chunk of level k_em (index into ch_em / ch_seg), -2: nothing.
+    // mark_end: record the timing mark after the last launch (one mark per launch slot).
+    auto level = [&](int k_ops, int k_em, int t0, int nt, bool split, int64_t ops_lo = -1, int64_t ops_hi = -1,
+                     int64_t em_part = -1, bool mark_end = true) {
         SweepArgs s = a;
         s.t0 = t0;
         LevelArgs L{};
@@ -832,7 +862,7 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
         int emit = lc.emit, chunk = lc.chunk, ops_cap = kOpsCtasPerSm[0];
         bool by_chunk = false;
         if (!lc.lv.empty() && slot < (int)lc.lv.size()) {
-            const int v = (lc.lv[slot] & ~GMR_LEVEL_PUSH) % GMR_N_LEVEL_VARIANTS;
+            const int v = (lc.lv[slot] & ~(GMR_LEVEL_PUSH | GMR_LEVEL_INTERLEAVE)) % GMR_N_LEVEL_VARIANTS;
             emit = kEmitVariants[v % kNumEmitVariants].emit;
             chunk = kEmitVariants[v % kNumEmitVariants].chunk;
             ops_cap = kOpsCtasPerSm[(v / kNumEmitVariants) % 2];
@@ -840,8 +870,15 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
         }
         if (lc.variant == GMR_VARIANT_PLAIN) emit = GMR_EMIT_ATOMIC;
         // level k_em pushed its emissions in its own launch: nothing to fold
-        if (k_em >= 1 && push_level(e, lc, k_em)) k_em = -1;
-        if (k_ops >= 1 && push_level(e, lc, k_ops)) {
+        if (k_em >= 1 && em_part == -1 && level_mode(e, lc, k_em) == kFoldPush) k_em = -1;
+        if (em_part == -2) k_em = -1;
+        // level k_em was interleaved: only its last source chunk is left to fold
+        if (k_em >= 1 && em_part == -1 && level_mode(e, lc, k_em) == kFoldInterleave) {
+            const int64_t r = interleave_chunks(e, k_em) - 1, nec = e->ch_off[k_em + 1] - e->ch_off[k_em];
+            if (r < nec) em_part = e->ch_off[k_em] + r;
+            else k_em = -1;
+        }
+        if (k_ops >= 1 && level_mode(e, lc, k_ops) == kFoldPush) {
             L.pe_off = static_cast<const int32_t*>(e->pe_off.p);
             L.pe_row = static_cast<const int32_t*>(e->pe_row.p);
             if (emit == GMR_EMIT_ROWS) emit = GMR_EMIT_SEGMENTED;  // the pushes are atomics into the same Y
@@ -855,10 +892,20 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
         L.em_chunk = chunk;
         int64_t nops = 0, nem = 0, nseg = 0;
         if (k_ops >= 1) {
-            L.op_first = e->lvl_off[k_ops - 1];
-            nops = e->lvl_off[k_ops] - e->lvl_off[k_ops - 1];
+            L.op_first = ops_lo >= 0 ? ops_lo : e->lvl_off[k_ops - 1];
+            nops = (ops_lo >= 0 ? ops_hi : e->lvl_off[k_ops]) - L.op_first;
         }
-        if (k_em >= 0) {
+        if (k_em >= 0 && em_part >= 0) {  // one source chunk, from the chunked emission order
+            L.em_src = static_cast<const int32_t*>(e->em_src_c.p);
+            L.em_row = static_cast<const int32_t*>(e->em_row_c.p);
+            L.seg_row = static_cast<const int32_t*>(e->seg_row_c.p);
+            L.seg_start = static_cast<const int64_t*>(e->seg_start_c.p);
+            L.em_first = e->ch_em[em_part];
+            nem = e->ch_em[em_part + 1] - e->ch_em[em_part];
+            L.seg_first = e->ch_seg[em_part];
+            nseg = e->ch_seg[em_part + 1] - e->ch_seg[em_part];
+            by_chunk = false;
+        } else if (k_em >= 0) {
             L.em_first = e->em_off[k_em];
             nem = e->em_off[k_em + 1] - e->em_off[k_em];
             L.seg_first = e->seg_off[k_em];
@@ -875,6 +922,7 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
             M.n_ops = no;
             M.n_em = ne;
             M.n_seg = ns;
+            mark = mark && mark_end;
             if (no == 0 && ne == 0) {
                 if (t_timer && mark && !split) t_timer->mark();  // keep one timing slot per level launch
                 return;
@@ -924,7 +972,21 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
         const int K = lc.ntile > 1 ? std::min(lc.tile_levels, D) : 0;
         for (int t = 0; t < (K > 0 ? lc.ntile : 0); ++t)
             for (int k = 1; k <= K; ++k) level(k, k - 1, t, 1, false);
-        for (int k = K + 1; k <= D; ++k) level(k, k - 1, 0, lc.ntile, false);
+        for (int k = K + 1; k <= D; ++k) {
+            if (level_mode(e, lc, k) != kFoldInterleave) {
+                level(k, k - 1, 0, lc.ntile, false);
+                continue;
+            }
+            // level k in source chunks: launch c evaluates chunk c and folds the
+            // emissions of chunk c - 1, whose values the previous launch left in L2
+            const int64_t base = e->lvl_off[k - 1], end = e->lvl_off[k], n_oc = interleave_chunks(e, k);
+            const int64_t nec = e->ch_off[k + 1] - e->ch_off[k];
+            for (int64_t c = 0; c < n_oc; ++c) {
+                const int64_t lo = base + c * e->chunk_slots, hi = std::min(end, lo + e->chunk_slots);
+                if (c == 0) level(k, k - 1, 0, lc.ntile, false, lo, hi, -1, n_oc == 1);
+                else level(k, k, 0, lc.ntile, false, lo, hi, c - 1 < nec ? e->ch_off[k] + c - 1 : -2, c == n_oc - 1);
+            }
+        }
         level(0, D, 0, lc.ntile, false);
     }
     GMR_CUDA(cudaGetLastError());
@@ -1071,7 +1133,7 @@ static Launch resolve_launch(gmr_engine* e, int semiring, int B, const void* X, 
     lc.emit = cfg && cfg->emit_mode ? cfg->emit_mode : GMR_EMIT_SEGMENTED;
     if (lc.variant == GMR_VARIANT_PLAIN) lc.emit = GMR_EMIT_ATOMIC;
     lc.push_mode = cfg ? cfg->push : GMR_PUSH_AUTO;
-    if (lc.push_mode < GMR_PUSH_AUTO || lc.push_mode > GMR_PUSH_ALWAYS) throw Error(GMR_ERR_ARG, "unknown push mode");
+    if (lc.push_mode < GMR_PUSH_AUTO || lc.push_mode > GMR_PUSH_INTERLEAVE) throw Error(GMR_ERR_ARG, "unknown push mode");
     lc.chunk = cfg && cfg->ops_per_cta > 0 ? cfg->ops_per_cta : 16;
     int bt = cfg && cfg->vec_tile > 0 ? cfg->vec_tile : auto_tile(e, lc.Bw);
     if (bt > lc.Bw || lc.Bw % bt != 0) bt = lc.Bw;  // tiles must divide the batch
@@ -1197,6 +1259,7 @@ static void build_chunked_emissions(const gmr_plan& p, gmr_engine& e) {
         long long v = std::atoll(env);
         if (v >= 1) kChunkSlots = v;
     }
+    e.chunk_slots = kChunkSlots;
     bool any = false;
     for (int k = 0; k <= D && !any; ++k) {
         const int64_t width = k == 0 ? p.n_terms() : p.lvl_off[k] - p.lvl_off[k - 1];
@@ -1477,8 +1540,12 @@ extern "C" int gmr_engine_set_level_variants(gmr_engine* e, int semiring, int B,
             return;
         }
         if (n != e->depth + 2) throw Error(GMR_ERR_ARG, "need depth + 2 = " + std::to_string(e->depth + 2) + " entries");
-        for (int i = 0; i < n; ++i)
-            if ((v[i] & ~GMR_LEVEL_PUSH) >= GMR_N_LEVEL_VARIANTS) throw Error(GMR_ERR_ARG, "variant index out of range");
+        for (int i = 0; i < n; ++i) {
+            if ((v[i] & ~(GMR_LEVEL_PUSH | GMR_LEVEL_INTERLEAVE)) >= GMR_N_LEVEL_VARIANTS)
+                throw Error(GMR_ERR_ARG, "variant index out of range");
+            if ((v[i] & GMR_LEVEL_PUSH) && (v[i] & GMR_LEVEL_INTERLEAVE))
+                throw Error(GMR_ERR_ARG, "a level cannot both push and interleave");
+        }
         e->level_variants[{semiring, B}] = std::vector<uint8_t>(v, v + n);
     });
 }
@@ -1555,17 +1622,21 @@ extern "C" int gmr_engine_autotune_energy(gmr_engine* e, int semiring, const voi
                 b = twin;
             best[l] = (uint8_t)b;
         }
-        // Push or pull, per level.  Slot k costs o_k (rules of level k) +
-        // p_k (if level k pushes) + f_{k-1} (if level k-1 does not push).
-        // Four tables measure it: none pushing (o_k + f_{k-1}), all pushing
-        // (o_k + p_k), odd levels pushing and even levels pushing (o_k alone in
-        // every slot whose level pushes nothing while the level below does).
-        // Level k pushes when p_k < f_k.  A level whose emissions cannot be
-        // pushed is never flagged, and the formulas stay exact around it.
+        // How each level's emissions reach Y: pull, push or interleave.  Slot k's
+        // time depends on the modes of levels k-1 (what is left to fold) and k
+        // (what its own launches do), slot depth+1's on level depth's.  Nine
+        // tables, mode a on odd levels and b on even ones for every ordered
+        // pair (a, b), time every slot under every pair of neighbouring modes;
+        // a pass over the levels then picks the cheapest chain of modes.
         const int D = e->depth;
-        bool can_push = false;
-        for (int k = 1; k <= D && k < (int)e->push_ok.size(); ++k) can_push |= e->push_ok[k] != 0;
-        if (can_push && D >= 1) {
+        const Launch lc0 = resolve_launch(e, semiring, B, dX, dY, nullptr);
+        auto allowed = [&](int k, int m) {
+            if (m == kFoldPull) return true;
+            return m == kFoldPush ? can_push(e, k) : can_interleave(e, lc0, k);
+        };
+        bool any_mode = false;
+        for (int k = 1; k <= D; ++k) any_mode |= allowed(k, kFoldPush) || allowed(k, kFoldInterleave);
+        if (any_mode) {
             auto slot_times = [&](const std::vector<uint8_t>& table) {
                 if (gmr_engine_set_level_variants(e, semiring, B, table.data(), nl) != GMR_OK)
                     throw Error(GMR_ERR_ARG, gmr_last_error());
@@ -1587,20 +1658,50 @@ extern "C" int gmr_engine_autotune_energy(gmr_engine* e, int semiring, const voi
                 }
                 return out;
             };
-            auto with_push = [&](int parity) {  // -1: every level; 0 / 1: even / odd levels
-                std::vector<uint8_t> t = best;
-                for (int k = 1; k <= D; ++k)
-                    if (parity < 0 || (k & 1) == parity) t[k] |= GMR_LEVEL_PUSH;
-                return t;
-            };
-            const std::vector<float> t0 = slot_times(best), t1 = slot_times(with_push(-1));
-            const std::vector<float> todd = slot_times(with_push(1)), teven = slot_times(with_push(0));
-            auto ops_only = [&](int k) { return (k & 1) ? teven[k] : todd[k]; };
-            for (int k = 1; k <= D; ++k) {
-                if (k >= (int)e->push_ok.size() || !e->push_ok[k]) continue;
-                const float pk = t1[k] - ops_only(k);
-                const float fk = k < D ? t0[k + 1] - ops_only(k + 1) : t0[D + 1];
-                if (pk < fk) best[k] |= GMR_LEVEL_PUSH;
+            const uint8_t flag[3] = {0, GMR_LEVEL_PUSH, GMR_LEVEL_INTERLEAVE};
+            const float kUnset = -1.0f;
+            // cost[k][3 * m_prev + m]: slot k with level k-1 in m_prev and level k in m
+            std::vector<std::array<float, 9>> cost(nl);
+            for (auto& c : cost) c.fill(kUnset);
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) {
+                    std::vector<uint8_t> t = best;
+                    std::vector<int> eff(D + 2, kFoldPull);
+                    for (int k = 1; k <= D; ++k) {
+                        const int m = (k & 1) ? a : b;
+                        eff[k] = allowed(k, m) ? m : kFoldPull;
+                        t[k] |= flag[eff[k]];
+                    }
+                    const std::vector<float> tt = slot_times(t);
+                    for (int k = 1; k <= D + 1; ++k) {
+                        const int m = k <= D ? eff[k] : kFoldPull;
+                        float& c = cost[k][3 * eff[k - 1] + m];
+                        c = c == kUnset ? tt[k] : std::min(c, tt[k]);
+                    }
+                }
+            const float kInf = 3.0e38f;
+            std::vector<std::array<float, 3>> acc(D + 2);
+            std::vector<std::array<int, 3>> from(D + 2);
+            for (auto& x : acc) x.fill(kInf);
+            acc[0][kFoldPull] = 0.0f;
+            for (int k = 1; k <= D + 1; ++k)
+                for (int m = 0; m < 3; ++m) {
+                    if (k <= D ? !allowed(k, m) : m != kFoldPull) continue;
+                    for (int mp = 0; mp < 3; ++mp) {
+                        const float c = cost[k][3 * mp + m];
+                        if (acc[k - 1][mp] >= kInf || c == kUnset) continue;
+                        if (acc[k - 1][mp] + c < acc[k][m]) {
+                            acc[k][m] = acc[k - 1][mp] + c;
+                            from[k][m] = mp;
+                        }
+                    }
+                }
+            if (acc[D + 1][kFoldPull] < kInf) {
+                int m = from[D + 1][kFoldPull];
+                for (int k = D; k >= 1; --k) {
+                    best[k] |= flag[m];
+                    m = from[k][m];
+                }
             }
         }
         if (gmr_engine_set_level_variants(e, semiring, B, best.data(), nl) != GMR_OK) throw Error(GMR_ERR_ARG, gmr_last_error());

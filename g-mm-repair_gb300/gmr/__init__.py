@@ -30,8 +30,8 @@ TROPICAL_INF = 1_000_000_000
 
 VARIANT_AUTO, VARIANT_PLAIN, VARIANT_FUSED, VARIANT_GRAPH, VARIANT_PERSISTENT = 0, 1, 2, 3, 4
 EMIT_AUTO, EMIT_ATOMIC, EMIT_SEGMENTED, EMIT_ROWS = 0, 1, 2, 3
-PUSH_AUTO, PUSH_NEVER, PUSH_ALWAYS = 0, 1, 2
-LEVEL_PUSH = 32
+PUSH_AUTO, PUSH_NEVER, PUSH_ALWAYS, PUSH_INTERLEAVE = 0, 1, 2, 3
+LEVEL_PUSH, LEVEL_INTERLEAVE = 32, 64
 
 __all__ = [
     "GmrError", "Csrv", "Grammar", "Plan", "Engine", "gen_mosaic", "gen_copy_graph", "repair", "semiring_id",

@@ -243,9 +243,10 @@ typedef struct {
                          the rows that emit them (see GMR_LEVEL_PUSH) */
 } gmr_config;
 enum {
-    GMR_PUSH_AUTO = 0,   /* the installed per-launch table, else the engine's rule */
-    GMR_PUSH_NEVER = 1,  /* every level's emissions are gathered by the next launch */
-    GMR_PUSH_ALWAYS = 2  /* every level that can push does */
+    GMR_PUSH_AUTO = 0,       /* the installed per-launch table, else the engine's rule */
+    GMR_PUSH_NEVER = 1,      /* every level's emissions are gathered by the next launch */
+    GMR_PUSH_ALWAYS = 2,     /* every level that can push does */
+    GMR_PUSH_INTERLEAVE = 3  /* every level that can interleaves (GMR_LEVEL_INTERLEAVE) */
 };
 enum {
     GMR_VARIANT_AUTO = 0,
@@ -297,10 +298,16 @@ int gmr_engine_time_launches(gmr_engine* e, int semiring, const void* dX, void* 
  * level k push their values into the rows that emit them as soon as they are
  * computed (vector reductions into Y, which stays in L2), so launch k+1
  * gathers nothing of level k; a launch that pushes folds level k-1 with
- * atomics (a row-owned fold there becomes the segmented one).
+ * atomics (a row-owned fold there becomes the segmented one).  Adding
+ * GMR_LEVEL_INTERLEAVE instead evaluates level k in source chunks (2^19
+ * slots, the chunks of c = 1 above), one launch per chunk, each launch also
+ * folding the emissions of the chunk before it while that chunk's values are
+ * still in L2; launch k+1 folds the last chunk.  Levels of one chunk, and
+ * levels that run tile by tile, ignore the flag.
  * n = depth + 2; v = NULL clears. */
 #define GMR_N_LEVEL_VARIANTS 20
 #define GMR_LEVEL_PUSH 32
+#define GMR_LEVEL_INTERLEAVE 64
 int gmr_engine_set_level_variants(gmr_engine* e, int semiring, int B, const uint8_t* v, int n);
 int gmr_engine_get_level_variants(const gmr_engine* e, int semiring, int B, uint8_t* v, int cap, int* n);
 /* Exhaustive autotuner: times every variant on every launch (median of

@@ -127,6 +127,7 @@ def test_direct_terminal_emissions(case, sr, B, monkeypatch):
     variant, the per-launch tables (chunked ones included) and the
     persistent kernel still match the oracle."""
     monkeypatch.setenv("GMR_DIRECT_TERMS", "1")
+    monkeypatch.setenv("GMR_CHUNK_SLOTS", "5")  # several source chunks per level: interleaving applies
     rows, cols = int(case["rows"]), int(case["cols"])
     X = random_X(sr, cols, B, 500 + B)
     ref = oracle_columns(case["sched"], sr, case["V"], X, rows, cols)
@@ -135,7 +136,7 @@ def test_direct_terminal_emissions(case, sr, B, monkeypatch):
     for cfg in CONFIGS:
         check(sr, engine_outputs(sr, eng.multiply(Xw, sr, B=B, **cfg), B), ref)
     rng = np.random.default_rng(B)
-    for table in ([v] * (eng.depth + 2) for v in (0, 3, 4, 10, 13, 32, 35, 45)):
+    for table in ([v] * (eng.depth + 2) for v in (0, 3, 4, 10, 13, 32, 35, 45, 64, 67, 77)):
         eng.set_level_variants(sr, B, table)
         check(sr, engine_outputs(sr, eng.multiply(Xw, sr, B=B), B), ref)
     eng.set_level_variants(sr, B, rng.integers(0, eng.N_LEVEL_VARIANTS, eng.depth + 2))
@@ -223,8 +224,9 @@ def test_autotuned_and_mixed_tables(case, sr):
     times = eng.autotune(sr, dX.data_ptr(), dY.data_ptr(), B)
     assert times.shape == (eng.depth + 2, eng.N_LEVEL_VARIANTS) and np.all(times[1:] > 0)
     best = eng.level_variants(sr, B)
-    assert best is not None and np.array_equal(best[1:] & (255 - gmr.LEVEL_PUSH), times[1:].argmin(axis=1))
-    assert not np.any(best[[0, eng.depth + 1]] & gmr.LEVEL_PUSH)  # only levels 1..depth can push
+    modes = gmr.LEVEL_PUSH | gmr.LEVEL_INTERLEAVE
+    assert best is not None and np.array_equal(best[1:] & (255 - modes), times[1:].argmin(axis=1))
+    assert not np.any(best[[0, eng.depth + 1]] & modes)  # only levels 1..depth push or interleave
     rng = np.random.default_rng(sr)
     mixed = rng.integers(0, eng.N_LEVEL_VARIANTS, eng.depth + 2) | (rng.random(eng.depth + 2) < 0.5) * gmr.LEVEL_PUSH
     for table in (best, rng.integers(0, eng.N_LEVEL_VARIANTS, eng.depth + 2), mixed):
@@ -253,7 +255,7 @@ def test_energy_aware_autotune(case, sr):
     for slot in range(1, eng.depth + 2):
         b = int(times[slot].argmin())
         want = b + 10 if b < 10 and times[slot, b + 10] <= times[slot, b] * (1 + tol) else b
-        assert table[slot] & (255 - gmr.LEVEL_PUSH) == want
+        assert table[slot] & (255 - gmr.LEVEL_PUSH - gmr.LEVEL_INTERLEAVE) == want
     check(sr, engine_outputs(sr, eng.multiply(Xw, sr, B=B), B), ref)
     with pytest.raises(gmr.GmrError):
         eng.autotune(sr, dX.data_ptr(), dY.data_ptr(), B, energy_tolerance=1.5)
@@ -320,10 +322,30 @@ def test_chunked_emission_passes(case, sr, monkeypatch):
     for B in (1, 32):
         X = random_X(sr, cols, B, 300 + B)
         ref = oracle_columns(case["sched"], sr, case["V"], X, rows, cols)
-        for v in (10, 12, 13, 14, 17, 42, 45):  # chunked: segmented 16 / 32, row-owned, atomic; 4 CTAs per SM; pushed
+        # chunked: segmented 16 / 32, row-owned, atomic; 4 CTAs per SM; pushed; interleaved
+        for v in (10, 12, 13, 14, 17, 42, 45, 64, 67, 68, 74, 77, 3 + 64):
             eng.set_level_variants(sr, B, np.full(eng.depth + 2, v, dtype=np.uint8))
             Y = engine_outputs(sr, eng.multiply(engine_inputs(sr, X), sr, B=B), B)
             check(sr, Y, ref)
+        rng = np.random.default_rng(sr + B)
+        for _ in range(3):  # mixed pull / push / interleave chains
+            modes = rng.choice([0, gmr.LEVEL_PUSH, gmr.LEVEL_INTERLEAVE], eng.depth + 2)
+            eng.set_level_variants(sr, B, rng.integers(0, eng.N_LEVEL_VARIANTS, eng.depth + 2) | modes)
+            check(sr, engine_outputs(sr, eng.multiply(engine_inputs(sr, X), sr, B=B), B), ref)
+        eng.set_level_variants(sr, B, None)
+        for cfg in (dict(push=gmr.PUSH_INTERLEAVE), dict(push=gmr.PUSH_INTERLEAVE, emit_mode=gmr.EMIT_ROWS),
+                    dict(push=gmr.PUSH_INTERLEAVE, variant=gmr.VARIANT_FUSED, emit_mode=gmr.EMIT_ATOMIC)):
+            check(sr, engine_outputs(sr, eng.multiply(engine_inputs(sr, X), sr, B=B, **cfg), B), ref)
+    # the autotuner's chain of pull / push / interleave choices keeps the results
+    torch = pytest.importorskip("torch")
+    B = 32
+    X = random_X(sr, cols, B, 333)
+    Xw = engine_inputs(sr, X)
+    dX = torch.from_numpy(Xw.view(np.int32)).cuda()
+    dY = torch.empty((rows, Xw.shape[1]), dtype=torch.int32, device="cuda")
+    eng.autotune(sr, dX.data_ptr(), dY.data_ptr(), B)
+    check(sr, engine_outputs(sr, eng.multiply(Xw, sr, B=B), B), oracle_columns(case["sched"], sr, case["V"], X,
+                                                                               rows, cols))
 
 
 def test_allocation_failure_is_reported():
