@@ -541,7 +541,10 @@ def cusparse_baseline(torch, args, rows, cols, B, n=20):
 
 def run_pack8(args):
     """Eight mosaic grammars of uneven size (rows ~U{5k..200k}, cols ~U{1k..10k},
-    seeds 10-17), each with its own B in {1, 4, 16, 64}, in one graph launch."""
+    seeds 10-17), each with its own B in {1, 4, 16, 64}, packed into one graph
+    launch of per-engine branches (the default pack mode).  The same pack as
+    one launch per level over all grammars, as one persistent kernel, and the
+    engines one after another are timed beside it."""
     import torch
 
     import gmr
@@ -582,6 +585,20 @@ def run_pack8(args):
         packed()
         sequential()
     ms_seq = timed_loop(torch, stream, sequential, args.steps)
+    pack.set_mode(gmr.Pack.LEVELS)  # one launch per level over all grammars
+    for _ in range(args.warmup):
+        packed()
+    ms_levels = timed_loop(torch, stream, packed, args.steps)
+    pack.set_mode(gmr.Pack.PERSISTENT)  # one cooperative kernel for the whole pack
+    for _ in range(args.warmup):
+        packed()
+    ms_persistent = timed_loop(torch, stream, packed, args.steps)
+    torch.cuda.synchronize()
+    persistent_ran = pack.status()[0]
+    pack.set_mode(gmr.Pack.GRAPH)  # the headline: the default, one graph of per-engine branches
+    for _ in range(args.warmup):
+        packed()
+    torch.cuda.synchronize()
     sampler = ClockSampler(0)
     sampler.start()
     time.sleep(0.3)
@@ -604,6 +621,10 @@ def run_pack8(args):
            "config": {"workload": "pack8", "grammars": info, "seeds": list(range(10, 18)),
                       "l2": "inputs larger than L2; no flush"},
            "sequential_vps": vecs * 1000.0 / ms_seq, "pack_gain": ms_seq / ms,
+           "mode": "one graph launch of per-engine branches (default pack mode)",
+           "levels_pack_vps": vecs * 1000.0 / ms_levels, "levels_pack_gain": ms_seq / ms_levels,
+           "persistent_pack_vps": vecs * 1000.0 / ms_persistent, "persistent_pack_gain": ms_seq / ms_persistent,
+           "persistent_ran": persistent_ran,
            "step_alg_gbs": total_alg / (ms / 1000.0) / 1e9, "gpu_launches": int(pack.last_launches * args.steps),
            "clocks": clocks, "check": check}
     print(json.dumps(out), flush=True)

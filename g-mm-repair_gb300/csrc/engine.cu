@@ -635,6 +635,129 @@ __global__ void __launch_bounds__(256) k_persistent(SweepArgs a, LevelArgs L0, P
     }
 }
 
+// Several grammars in ONE persistent launch.  Each grammar brings its own
+// plan, scratch, X, Y and batch width (its lane layout is `kind`, a
+// (VEC, GLOG) class); phase k runs level k of every grammar that still has
+// one (rules of level k, emissions of level k-1; phase 0 the prologues),
+// every grammar over the whole grid one after another, so a small grammar's
+// few rules fill the threads a big grammar leaves idle.  One bounded grid
+// barrier separates the phases.
+struct PackGrammar {
+    SweepArgs a;
+    LevelArgs L;  // level-independent fields (arrays, chunk)
+    const int64_t* lvl_off;
+    const int64_t* em_off;
+    const int64_t* seg_off;
+    int depth;
+    int kind;     // 0-6: VEC 4 with GLOG 0..5 / generic; 7, 8: VEC 2 / 1 with G = 1; 9, 10: VEC 2 / 1 generic
+};
+
+// The grammar's argument structs are copied into locals first: read through
+// a pointer they would be reloaded from global memory inside the loops.
+template <class S, int VEC, int GLOG, int EMIT>
+__device__ __forceinline__ void pack_phase(const PackGrammar& g, int k, int64_t t0, int64_t stride) {
+    const SweepArgs a = g.a;
+    if (k == 0) {
+        do_prologue<S, VEC, GLOG>(a, 0, t0, stride);
+        return;
+    }
+    LevelArgs L = g.L;
+    if (k <= g.depth) {
+        L.op_first = g.lvl_off[k - 1];
+        L.n_ops = g.lvl_off[k] - g.lvl_off[k - 1];
+    } else {
+        L.n_ops = 0;
+    }
+    L.em_first = g.em_off[k - 1];
+    L.n_em = g.em_off[k] - g.em_off[k - 1];
+    L.seg_first = g.seg_off[k - 1];
+    L.n_seg = g.seg_off[k] - g.seg_off[k - 1];
+    emits_t<S, VEC, GLOG, EMIT, true, false>(a, L, 0, t0, stride);
+    do_ops<S, VEC, GLOG, true, false>(a, L, 0, t0, stride);
+}
+
+template <class S, int EMIT>
+__global__ void __launch_bounds__(256) k_pack(const PackGrammar* __restrict__ gs, int n, int max_depth, PersistArgs P) {
+    const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int k = 0; k <= max_depth + 1; ++k) {
+        for (int i = 0; i < n; ++i) {
+            const PackGrammar& g = gs[i];
+            if (k > g.depth + 1) continue;
+            switch (g.kind) {
+                case 0: pack_phase<S, 4, 0, EMIT>(g, k, t0, stride); break;
+                case 1: pack_phase<S, 4, 1, EMIT>(g, k, t0, stride); break;
+                case 2: pack_phase<S, 4, 2, EMIT>(g, k, t0, stride); break;
+                case 3: pack_phase<S, 4, 3, EMIT>(g, k, t0, stride); break;
+                case 4: pack_phase<S, 4, 4, EMIT>(g, k, t0, stride); break;
+                case 5: pack_phase<S, 4, 5, EMIT>(g, k, t0, stride); break;
+                case 6: pack_phase<S, 4, -1, EMIT>(g, k, t0, stride); break;
+                case 7: pack_phase<S, 2, 0, EMIT>(g, k, t0, stride); break;
+                case 8: pack_phase<S, 1, 0, EMIT>(g, k, t0, stride); break;
+                case 9: pack_phase<S, 2, -1, EMIT>(g, k, t0, stride); break;
+                default: pack_phase<S, 1, -1, EMIT>(g, k, t0, stride); break;
+            }
+        }
+        if (!grid_barrier(P, k)) return;
+    }
+}
+
+// The same pack as one launch per level (GMR_PACK_LEVELS): launch k covers
+// level k of every grammar, grammar i on blocks [blk[i], blk[i+1]), the first
+// em_blocks[i] of them folding its emissions of level k-1 and the rest
+// evaluating its rules of level k (k = 0: the prologues).  Plain cached loads:
+// launch boundaries order the levels.
+static constexpr int kMaxPackLevels = 32;  // grammars per pack in this mode
+struct PackLaunch {
+    int n, k;
+    int blk[kMaxPackLevels + 1];
+    int em_blocks[kMaxPackLevels];
+};
+
+template <class S, int VEC, int GLOG, int EMIT>
+__device__ __forceinline__ void pack_level_part(const PackGrammar& g, int k, int b, int nb, int eb) {
+    const int64_t tid = threadIdx.x;
+    const SweepArgs a = g.a;
+    if (k == 0) {
+        do_prologue<S, VEC, GLOG>(a, 0, (int64_t)b * blockDim.x + tid, (int64_t)nb * blockDim.x);
+        return;
+    }
+    LevelArgs L = g.L;
+    if (k <= g.depth) {
+        L.op_first = g.lvl_off[k - 1];
+        L.n_ops = g.lvl_off[k] - g.lvl_off[k - 1];
+    } else {
+        L.n_ops = 0;
+    }
+    L.em_first = g.em_off[k - 1];
+    L.n_em = g.em_off[k] - g.em_off[k - 1];
+    L.seg_first = g.seg_off[k - 1];
+    L.n_seg = g.seg_off[k] - g.seg_off[k - 1];
+    if (b < eb) emits_t<S, VEC, GLOG, EMIT, false, false>(a, L, 0, (int64_t)b * blockDim.x + tid, (int64_t)eb * blockDim.x);
+    else do_ops<S, VEC, GLOG, false, false>(a, L, 0, (int64_t)(b - eb) * blockDim.x + tid, (int64_t)(nb - eb) * blockDim.x);
+}
+
+template <class S, int EMIT>
+__global__ void __launch_bounds__(256) k_pack_level(const PackGrammar* __restrict__ gs, PackLaunch P) {
+    int i = 0;
+    while (i + 1 < P.n && (int)blockIdx.x >= P.blk[i + 1]) ++i;
+    const PackGrammar& g = gs[i];
+    const int b = (int)blockIdx.x - P.blk[i], nb = P.blk[i + 1] - P.blk[i], eb = P.em_blocks[i];
+    switch (g.kind) {
+        case 0: pack_level_part<S, 4, 0, EMIT>(g, P.k, b, nb, eb); break;
+        case 1: pack_level_part<S, 4, 1, EMIT>(g, P.k, b, nb, eb); break;
+        case 2: pack_level_part<S, 4, 2, EMIT>(g, P.k, b, nb, eb); break;
+        case 3: pack_level_part<S, 4, 3, EMIT>(g, P.k, b, nb, eb); break;
+        case 4: pack_level_part<S, 4, 4, EMIT>(g, P.k, b, nb, eb); break;
+        case 5: pack_level_part<S, 4, 5, EMIT>(g, P.k, b, nb, eb); break;
+        case 6: pack_level_part<S, 4, -1, EMIT>(g, P.k, b, nb, eb); break;
+        case 7: pack_level_part<S, 2, 0, EMIT>(g, P.k, b, nb, eb); break;
+        case 8: pack_level_part<S, 1, 0, EMIT>(g, P.k, b, nb, eb); break;
+        case 9: pack_level_part<S, 2, -1, EMIT>(g, P.k, b, nb, eb); break;
+        default: pack_level_part<S, 1, -1, EMIT>(g, P.k, b, nb, eb); break;
+    }
+}
+
 // ------------------------------------------------------------------ engine
 // Fully resolved launch configuration of one multiply.
 // Kernel variants a k_level launch can use: emission folding strategy and
@@ -2143,7 +2266,204 @@ struct gmr_pack {
     std::vector<void*> key_y, key_arena;
     int64_t launches = 0;
     int device = 0;
+    // one persistent launch (GMR_PACK_PERSISTENT): grammar table on the
+    // device, barrier and error words, pinned copy of the error words
+    int mode = GMR_PACK_GRAPH;
+    unsigned long long spin_limit = 20000000ull;
+    cudaGraphExec_t levels_exec = nullptr;  // GMR_PACK_LEVELS: the captured level chain
+    int levels_semiring = -1;
+    int64_t levels_launches = 0;
+    gmr::DevBuf table, sync;
+    std::vector<char> key_table;
+    int* status_host = nullptr;
+    bool last_persistent = false;
 };
+
+namespace gmr {
+
+static int pack_kind(const Launch& lc) {
+    if (lc.VEC == 4) {
+        for (int l = 0; l <= 5; ++l)
+            if (lc.G == (1 << l)) return l;
+        return 6;
+    }
+    if (lc.VEC == 2) return lc.G == 1 ? 7 : 9;
+    return lc.G == 1 ? 8 : 10;
+}
+
+template <class S>
+static void launch_pack(gmr_pack* p, const PackGrammar* table, int n, int max_depth, cudaStream_t st) {
+    auto kernel = k_pack<S, GMR_EMIT_SEGMENTED>;
+    int per_sm = 0, sms = 152;
+    GMR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0));
+    if (per_sm < 1) throw Error(GMR_ERR_STATE, "packed persistent kernel cannot be resident");
+    GMR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
+    PersistArgs P{};
+    P.bar = static_cast<unsigned*>(p->sync.p);
+    P.err = reinterpret_cast<int*>(static_cast<unsigned char*>(p->sync.p) + 8);
+    P.spin_limit = p->spin_limit;
+    GMR_CUDA(cudaMemsetAsync(p->sync.p, 0, 16, st));
+    const PackGrammar* tb = table;
+    void* args[] = {&tb, &n, &max_depth, &P};
+    GMR_CUDA(cudaLaunchCooperativeKernel(reinterpret_cast<void*>(kernel), dim3(per_sm * sms), dim3(256), args, 0, st));
+    GMR_CUDA(cudaMemcpyAsync(p->status_host, P.err, 8, cudaMemcpyDeviceToHost, st));
+}
+
+// Grammar table of a pack (every engine in one semiring, no direct
+// terminals), uploaded again only when the engines' scratch, X, Y or widths
+// change.  Returns the deepest grammar's depth; *changed = a new upload.
+static int pack_table(gmr_pack* p, const std::vector<Launch>& lcs, const void* const* dX, void* const* dY,
+                      cudaStream_t st, std::vector<PackGrammar>& tab, bool* changed) {
+    const int n = (int)p->engines.size();
+    tab.assign(n, PackGrammar{});
+    int max_depth = 0;
+    for (int i = 0; i < n; ++i) {
+        gmr_engine* e = p->engines[i];
+        const Launch& lc = lcs[i];
+        PackGrammar& g = tab[i];
+        std::memset(static_cast<void*>(&g), 0, sizeof(g));
+        SweepArgs& a = g.a;
+        a.arena = e->arena.p;
+        a.T = e->T.p;
+        a.Y = dY[i];
+        a.X = dX[i];
+        a.V = static_cast<const float*>(e->V.p);
+        a.term_val = static_cast<const int32_t*>(e->term_val.p);
+        a.term_col = static_cast<const int32_t*>(e->term_col.p);
+        a.n_terms = e->n_terms;
+        a.n_ops = e->n_ops;
+        a.rows = e->rows;
+        a.ldx = lc.Bw;
+        a.ldy = lc.Bw;
+        a.Bt = lc.Bw;
+        a.G = lc.Bw / lc.VEC;
+        a.t0 = 0;
+        a.cols = e->cols;
+        LevelArgs& L = g.L;
+        L.ops = static_cast<const int2*>(e->ops.p);
+        L.op_c = e->has_coeff ? static_cast<const float*>(e->op_c.p) : nullptr;
+        L.em_src = static_cast<const int32_t*>(e->em_src.p);
+        L.em_row = static_cast<const int32_t*>(e->em_row.p);
+        L.seg_row = static_cast<const int32_t*>(e->seg_row.p);
+        L.seg_start = static_cast<const int64_t*>(e->seg_start.p);
+        L.em_chunk = 16;
+        g.lvl_off = static_cast<const int64_t*>(e->d_lvl_off.p);
+        g.em_off = static_cast<const int64_t*>(e->d_em_off.p);
+        g.seg_off = static_cast<const int64_t*>(e->d_seg_off.p);
+        g.depth = e->depth;
+        Launch one = lc;
+        one.Bt = lc.Bw;
+        one.G = a.G;
+        g.kind = pack_kind(one);
+        max_depth = std::max(max_depth, e->depth);
+    }
+    const size_t bytes = sizeof(PackGrammar) * (size_t)n;
+    std::vector<char> key(reinterpret_cast<const char*>(tab.data()), reinterpret_cast<const char*>(tab.data()) + bytes);
+    *changed = key != p->key_table;
+    if (*changed) {
+        p->table.ensure(bytes);
+        GMR_CUDA(cudaStreamSynchronize(st));  // the table may be in use by an earlier launch
+        GMR_CUDA(cudaMemcpy(p->table.p, tab.data(), bytes, cudaMemcpyHostToDevice));
+        p->key_table = std::move(key);
+    }
+    return max_depth;
+}
+
+static void pack_persistent(gmr_pack* p, int semiring, const std::vector<Launch>& lcs, const void* const* dX,
+                            void* const* dY, cudaStream_t st) {
+    std::vector<PackGrammar> tab;
+    bool changed = false;
+    const int n = (int)p->engines.size();
+    const int max_depth = pack_table(p, lcs, dX, dY, st, tab, &changed);
+    const PackGrammar* table = static_cast<const PackGrammar*>(p->table.p);
+    if (semiring == GMR_PLUS_TIMES) launch_pack<SPlus>(p, table, n, max_depth, st);
+    else if (semiring == GMR_BOOLEAN) launch_pack<SBool>(p, table, n, max_depth, st);
+    else launch_pack<STrop>(p, table, n, max_depth, st);
+    p->launches = 1;
+    p->last_persistent = true;
+}
+
+// Blocks of grammar g in the level-k launch: the engine's own grid sizing
+// (emissions folded by the segmented chunk-16 fold, rules two per thread,
+// at most 32 blocks per SM for each part, grid-stride beyond).
+static void pack_level_blocks(const gmr_engine* e, const PackGrammar& g, int k, int sm_count, int* eb, int* ob) {
+    auto blocks = [&](int64_t items) -> int {
+        return (int)std::max<int64_t>(1, std::min<int64_t>((items + 255) / 256, (int64_t)sm_count * 32));
+    };
+    const int G = g.a.G;
+    const bool lane_per_unit = g.kind == 0 || g.kind == 7 || g.kind == 8;  // warp-segmented fold
+    *eb = *ob = 0;
+    if (k == 0) {
+        *ob = blocks((e->rows + e->n_terms) * (int64_t)G);
+        return;
+    }
+    if (k > e->depth + 1) return;
+    const int64_t ne = e->em_off[k] - e->em_off[k - 1];
+    const int64_t no = k <= e->depth ? e->lvl_off[k] - e->lvl_off[k - 1] : 0;
+    if (ne > 0) *eb = blocks(lane_per_unit ? (ne + 1) / 2 : (ne + 15) / 16 * G);
+    if (no > 0) *ob = blocks((no * G + 1) / 2);
+}
+
+template <class S>
+static void pack_level_chain(gmr_pack* p, int n, int max_depth, cudaStream_t st) {
+    const PackGrammar* table = static_cast<const PackGrammar*>(p->table.p);
+    int sms = 152;
+    GMR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
+    std::vector<PackGrammar> host(n);
+    std::memcpy(static_cast<void*>(host.data()), p->key_table.data(), sizeof(PackGrammar) * (size_t)n);
+    int64_t launches = 0;
+    for (int k = 0; k <= max_depth + 1; ++k) {
+        PackLaunch P{};
+        P.n = n;
+        P.k = k;
+        for (int i = 0; i < n; ++i) {
+            int eb = 0, ob = 0;
+            pack_level_blocks(p->engines[i], host[i], k, sms, &eb, &ob);
+            P.em_blocks[i] = eb;
+            P.blk[i + 1] = P.blk[i] + eb + ob;
+        }
+        if (P.blk[n] == 0) continue;
+        k_pack_level<S, GMR_EMIT_SEGMENTED><<<P.blk[n], 256, 0, st>>>(table, P);
+        ++launches;
+    }
+    GMR_CUDA(cudaGetLastError());
+    p->launches = launches;
+}
+
+// The pack as one launch per level, captured once into a graph and replayed
+// while the grammar table stays the same.
+static void pack_levels(gmr_pack* p, int semiring, const std::vector<Launch>& lcs, const void* const* dX,
+                        void* const* dY, cudaStream_t st) {
+    std::vector<PackGrammar> tab;
+    bool changed = false;
+    const int n = (int)p->engines.size();
+    const int max_depth = pack_table(p, lcs, dX, dY, st, tab, &changed);
+    if (changed || !p->levels_exec || p->levels_semiring != semiring) {
+        if (p->levels_exec) cudaGraphExecDestroy(p->levels_exec);
+        p->levels_exec = nullptr;
+        cudaGraph_t graph = nullptr;
+        GMR_CUDA(cudaStreamBeginCapture(p->origin, cudaStreamCaptureModeThreadLocal));
+        try {
+            if (semiring == GMR_PLUS_TIMES) pack_level_chain<SPlus>(p, n, max_depth, p->origin);
+            else if (semiring == GMR_BOOLEAN) pack_level_chain<SBool>(p, n, max_depth, p->origin);
+            else pack_level_chain<STrop>(p, n, max_depth, p->origin);
+        } catch (...) {
+            cudaStreamEndCapture(p->origin, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            throw;
+        }
+        GMR_CUDA(cudaStreamEndCapture(p->origin, &graph));
+        cudaError_t ie = cudaGraphInstantiate(&p->levels_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        GMR_CUDA(ie);
+        p->levels_semiring = semiring;
+        p->levels_launches = p->launches;
+    }
+    GMR_CUDA(cudaGraphLaunch(p->levels_exec, st));
+    p->launches = p->levels_launches;
+}
+
+}  // namespace gmr
 
 extern "C" int gmr_pack_create(gmr_engine* const* engines, int n, gmr_pack** out) {
     return guarded([&] {
@@ -2162,6 +2482,10 @@ extern "C" int gmr_pack_create(gmr_engine* const* engines, int n, gmr_pack** out
         GMR_CUDA(cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming));
         p->join.resize(n);
         for (auto& ev : p->join) GMR_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        p->sync.ensure(16);
+        GMR_CUDA(cudaMemset(p->sync.p, 0, 16));
+        GMR_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&p->status_host), 16, cudaHostAllocDefault));
+        std::memset(p->status_host, 0, 16);
         *out = p.release();
     });
 }
@@ -2185,6 +2509,20 @@ extern "C" int gmr_pack_multiply(gmr_pack* p, const int* semirings, const void* 
             Launch lc = resolve_launch(e, semirings[i], B[i], dX[i], dY[i], nullptr);
             ensure_scratch(e, lc.Bw);
             lcs.push_back(lc);
+        }
+        bool uniform = true, direct = false;
+        for (int i = 0; i < n; ++i) {
+            uniform = uniform && semirings[i] == semirings[0];
+            direct = direct || p->engines[i]->direct_terms;
+        }
+        p->last_persistent = false;
+        if (p->mode == GMR_PACK_PERSISTENT && uniform && !direct) {
+            pack_persistent(p, semirings[0], lcs, dX, dY, static_cast<cudaStream_t>(stream));
+            return;
+        }
+        if (p->mode == GMR_PACK_LEVELS && uniform && !direct && n <= kMaxPackLevels) {
+            pack_levels(p, semirings[0], lcs, dX, dY, static_cast<cudaStream_t>(stream));
+            return;
         }
         bool hit = p->exec != nullptr && p->key_lc.size() == (size_t)n;
         for (int i = 0; hit && i < n; ++i)
@@ -2227,12 +2565,35 @@ extern "C" int gmr_pack_multiply(gmr_pack* p, const int* semirings, const void* 
 
 extern "C" int64_t gmr_pack_last_launches(const gmr_pack* p) { return p ? p->launches : -1; }
 
+extern "C" int gmr_pack_set_mode(gmr_pack* p, int mode, int spin_limit) {
+    return guarded([&] {
+        if (!p) throw Error(GMR_ERR_ARG, "null pack");
+        if (mode != GMR_PACK_GRAPH && mode != GMR_PACK_PERSISTENT && mode != GMR_PACK_LEVELS)
+            throw Error(GMR_ERR_ARG, "unknown pack mode");
+        p->mode = mode;
+        p->spin_limit = spin_limit > 0 ? (unsigned long long)spin_limit : 20000000ull;
+    });
+}
+
+extern "C" int gmr_pack_status(const gmr_pack* p, int* persistent, int* failed, int* phase) {
+    return guarded([&] {
+        if (!p) throw Error(GMR_ERR_ARG, "null pack");
+        if (persistent) *persistent = p->last_persistent ? 1 : 0;
+        if (failed) *failed = p->last_persistent ? p->status_host[0] : 0;
+        if (phase) *phase = p->last_persistent ? p->status_host[1] : 0;
+    });
+}
+
 extern "C" void gmr_pack_free(gmr_pack* p) {
     if (!p) return;
     int prev = -1;
     cudaGetDevice(&prev);
     cudaSetDevice(p->device);
     if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->levels_exec) cudaGraphExecDestroy(p->levels_exec);
+    p->table.release();
+    p->sync.release();
+    if (p->status_host) cudaFreeHost(p->status_host);
     for (auto ev : p->join) cudaEventDestroy(ev);
     if (p->fork) cudaEventDestroy(p->fork);
     if (p->origin) cudaStreamDestroy(p->origin);

@@ -548,6 +548,20 @@ class Pack:
         bs = (C.c_int * n)(*Bs)
         _check(lib().gmr_pack_multiply(self._h, sr, xs, ys, bs, C.c_void_p(stream)))
 
+    GRAPH, PERSISTENT, LEVELS = 0, 1, 2
+
+    def set_mode(self, mode: int, spin_limit: int = 0):
+        """Pack.GRAPH (default): one CUDA-graph launch of per-engine branches;
+        Pack.LEVELS: one launch per level over every grammar;
+        Pack.PERSISTENT: one cooperative kernel for the whole pack."""
+        _check(lib().gmr_pack_set_mode(self._h, int(mode), int(spin_limit)))
+
+    def status(self):
+        """(ran_persistent, failed, phase) of the last multiply (after a stream synchronize)."""
+        a, f, p = C.c_int(), C.c_int(), C.c_int()
+        _check(lib().gmr_pack_status(self._h, C.byref(a), C.byref(f), C.byref(p)))
+        return bool(a.value), f.value, p.value
+
     @property
     def last_launches(self) -> int:
         return int(lib().gmr_pack_last_launches(self._h))

@@ -129,6 +129,8 @@ _SIGS = {
     "gmr_pack_create": (C.c_int, [C.POINTER(P), C.c_int, C.POINTER(P)]),
     "gmr_pack_multiply": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(P), C.POINTER(P), C.POINTER(C.c_int), P]),
     "gmr_pack_last_launches": (C.c_int64, [P]),
+    "gmr_pack_set_mode": (C.c_int, [P, C.c_int, C.c_int]),
+    "gmr_pack_status": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "gmr_pack_free": (None, [P]),
     "gmr_engine_device_bytes": (C.c_int64, [P]),
     "gmr_engine_free": (None, [P]),

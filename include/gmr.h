@@ -408,8 +408,10 @@ int gmr_engine_fixpoint(gmr_engine* e, int semiring, void* dX, void* dY, int B, 
                         void* stream, int* iters);
 
 /* Several engines in one launch: grammars of uneven size, each with its own
- * semiring, X, Y and B, multiplied by one CUDA-graph launch that runs one
- * branch per engine concurrently (each branch = that engine's AUTO chain).
+ * semiring, X, Y and B.  By default (GMR_PACK_GRAPH) one CUDA-graph launch
+ * runs one branch per engine concurrently (each branch = that engine's AUTO
+ * chain, its own autotuned per-level variants); gmr_pack_set_mode selects the
+ * two single-kernel packings instead.
  * The graph is captured on the first call with a given set of arguments and
  * replayed afterwards.  All engines must live on the same device; an engine
  * may belong to one pack call at a time. */
@@ -418,6 +420,26 @@ int gmr_pack_create(gmr_engine* const* engines, int n, gmr_pack** out);
 int gmr_pack_multiply(gmr_pack* p, const int* semirings, const void* const* dX, void* const* dY,
                       const int* B, void* stream);
 int64_t gmr_pack_last_launches(const gmr_pack* p);
+/* How gmr_pack_multiply runs the pack.
+ *  GMR_PACK_GRAPH (the default): the graph of per-engine branches above.
+ *  GMR_PACK_LEVELS: one launch per level covers every grammar (level k of
+ *    each, on its own range of blocks sized by its work: rules of level k and
+ *    emissions of level k-1; launch 0 the prologues), depth of the deepest
+ *    grammar + 2 launches, captured once into a graph and replayed.  Up to 32
+ *    grammars.  Every grammar folds its emissions with the segmented fold.
+ *  GMR_PACK_PERSISTENT: ONE cooperative kernel launch walks every grammar:
+ *    phase k runs level k of every grammar that still has one, one grammar
+ *    after another over the whole grid, with one grid barrier between phases.
+ *    Each barrier wait gives up after spin_limit polls (0 = 20,000,000);
+ *    gmr_pack_status then reports it.
+ * LEVELS and PERSISTENT need one semiring for the whole pack and no engine
+ * with direct terminals; otherwise the graph of branches runs. */
+enum { GMR_PACK_GRAPH = 0, GMR_PACK_PERSISTENT = 1, GMR_PACK_LEVELS = 2 };
+int gmr_pack_set_mode(gmr_pack* p, int mode, int spin_limit);
+/* After the stream of the last gmr_pack_multiply has been synchronized:
+ * *persistent = 1 if it ran as one persistent launch (GMR_PACK_PERSISTENT), *failed != 0 if a
+ * grid-barrier wait gave up (the Y of that call are not valid), *phase = where. */
+int gmr_pack_status(const gmr_pack* p, int* persistent, int* failed, int* phase);
 void gmr_pack_free(gmr_pack* p);
 
 /* Kernel launches issued by the calling thread's last multiply. */

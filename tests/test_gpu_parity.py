@@ -306,9 +306,97 @@ def test_packed_multi_grammar_launch():
                              [a[1] for a in args], stream=torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     assert pack.last_launches >= 8 * 3
+    assert pack.status()[0] is False  # mixed semirings: the graph of per-engine branches
     for (sched, V, rows, cols), (sr, B, X, dX, dY) in zip(scheds, args):
         Yw = dY.cpu().numpy().view({0: np.float32, 1: np.uint32, 2: np.int32}[sr])
         check(sr, engine_outputs(sr, Yw, B), oracle_columns(sched, sr, V, X, rows, cols))
+
+
+PACK_WIDTHS = {0: [1, 3, 4, 16, 33, 64, 2, 8], 1: [1, 40, 64, 128, 200, 32, 7, 96], 2: [1, 3, 4, 16, 33, 64, 2, 8]}
+
+
+@pytest.fixture(scope="module")
+def pack_grammars():
+    rng = np.random.default_rng(12)
+    out = []
+    for i in range(8):
+        rows, cols = int(rng.integers(200, 4000)), int(rng.integers(64, 900))
+        m = gmr.gen_mosaic(rows, cols, 16, 0.02, 0.002, 30 + i, threads=4)
+        g = gmr.repair(m, 4)
+        out.append(dict(plan=gmr.Plan.build(g, rows, cols), sched=O.RefSchedule(g.alpha, g.rules(), g.C()),
+                        V=g.values(), rows=rows, cols=cols))
+    return out
+
+
+@pytest.mark.parametrize("sr", range(3))
+def test_packed_persistent_kernel(pack_grammars, sr):
+    """Eight uneven grammars in ONE persistent launch, and in one launch per
+    level over all of them (one semiring, each its own B, so every lane layout
+    of the kernels' grammar table is used)."""
+    torch = pytest.importorskip("torch")
+    engines, args = [], []
+    for i, gd in enumerate(pack_grammars):
+        engines.append(gmr.Engine(gd["plan"]))
+        B = PACK_WIDTHS[sr][i]
+        X = random_X(sr, gd["cols"], B, 70 + i)
+        Xw = engine_inputs(sr, X)
+        dX = torch.from_numpy(Xw.view(np.int32)).cuda()
+        dY = torch.full((gd["rows"], Xw.shape[1]), 7, dtype=torch.int32, device="cuda")
+        args.append((B, X, dX, dY))
+    pack = gmr.Pack(engines)
+    st = torch.cuda.current_stream().cuda_stream
+    max_depth = max(e.depth for e in engines)
+    for mode in (gmr.Pack.PERSISTENT, gmr.Pack.LEVELS):
+        pack.set_mode(mode)
+        for _ in range(2):  # table upload (and capture), then reuse
+            for a in args:
+                a[3].fill_(7)
+            pack.multiply_device([sr] * 8, [a[2].data_ptr() for a in args], [a[3].data_ptr() for a in args],
+                                 [a[0] for a in args], stream=st)
+            torch.cuda.synchronize()
+            if mode == gmr.Pack.PERSISTENT:
+                assert pack.status() == (True, 0, 0) and pack.last_launches == 1
+            else:
+                assert pack.status()[0] is False and pack.last_launches == max_depth + 2
+            for gd, (B, X, dX, dY) in zip(pack_grammars, args):
+                Yw = dY.cpu().numpy().view({0: np.float32, 1: np.uint32, 2: np.int32}[sr])
+                check(sr, engine_outputs(sr, Yw, B), oracle_columns(gd["sched"], sr, gd["V"], X, gd["rows"],
+                                                                    gd["cols"]))
+    pack.set_mode(gmr.Pack.GRAPH)  # the same call as a graph of branches
+    pack.multiply_device([sr] * 8, [a[2].data_ptr() for a in args], [a[3].data_ptr() for a in args],
+                         [a[0] for a in args], stream=st)
+    torch.cuda.synchronize()
+    assert pack.status()[0] is False
+
+
+def test_packed_persistent_barrier_timeout(pack_grammars):
+    """A barrier wait limited to one poll gives up and is reported; the next
+    call with the normal limit is correct again."""
+    torch = pytest.importorskip("torch")
+    engines = [gmr.Engine(gd["plan"]) for gd in pack_grammars]
+    B = 8
+    Xs = [random_X(0, gd["cols"], B, 90 + i) for i, gd in enumerate(pack_grammars)]
+    dXs = [torch.from_numpy(x).cuda() for x in Xs]
+    dYs = [torch.zeros((gd["rows"], B), dtype=torch.float32, device="cuda") for gd in pack_grammars]
+    pack = gmr.Pack(engines)
+    st = torch.cuda.current_stream().cuda_stream
+    call = lambda: pack.multiply_device([0] * 8, [x.data_ptr() for x in dXs], [y.data_ptr() for y in dYs],
+                                        [B] * 8, stream=st)
+    pack.set_mode(gmr.Pack.PERSISTENT, spin_limit=1)
+    failures = 0
+    for _ in range(3):
+        call()
+        torch.cuda.synchronize()
+        ran, failed, phase = pack.status()
+        assert ran
+        failures += failed != 0
+    assert failures >= 1
+    pack.set_mode(gmr.Pack.PERSISTENT)
+    call()
+    torch.cuda.synchronize()
+    assert pack.status() == (True, 0, 0)
+    for gd, X, dY in zip(pack_grammars, Xs, dYs):
+        check(0, dY.cpu().numpy(), oracle_columns(gd["sched"], 0, gd["V"], X, gd["rows"], gd["cols"]))
 
 
 @pytest.mark.parametrize("sr", range(3))
