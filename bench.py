@@ -705,6 +705,26 @@ def run_other_op(args):
     return 0
 
 
+def run_gather_sweep(args):
+    """The gather calibration along every load path: random 128-byte units
+    (and larger units for bulk copies) from a buffer that fits in L2 (64 MB)
+    and one that does not (4 GB), at several depths of loads in flight."""
+    import gmr
+
+    cases = ([("load16", d, 128) for d in (1, 2, 4, 8, 16)] + [("load32", d, 128) for d in (2, 4, 8)] +
+             [("seq16", d, 128) for d in (4, 16)] + [("bulk", d, 128) for d in (2, 4, 8, 16, 32)] +
+             [("bulk", 4, u) for u in (512, 2048, 8192)])
+    rows = []
+    for buf in (64 << 20, 4 << 30):
+        for mode, depth, unit in cases:
+            gbs = gmr.measure_gather(buf, mode=mode, depth=depth, unit_bytes=unit)
+            rows.append({"buffer_mb": buf >> 20, "mode": mode, "depth": depth, "unit_bytes": unit,
+                         "gbs": round(gbs, 1)})
+            print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
+    print(json.dumps({"op": "gather", "unit": "GB/s", "results": rows}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -729,9 +749,10 @@ def main():
     ap.add_argument("--no-cusparse", action="store_true", help="skip the cuSPARSE CSR baseline")
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="--impl reference: skip timing the reference's own GPU engine beside its CPU sweep")
-    ap.add_argument("--op", choices=["right", "left", "fixpoint", "repair"], default="right",
+    ap.add_argument("--op", choices=["right", "left", "fixpoint", "repair", "gather"], default="right",
                     help="right: Y = M X (the headline); left: Y = X^T M; fixpoint: X <- X (+) M X to convergence; "
-                         "repair: RePair of the workload's matrix on the GPU vs the host")
+                         "repair: RePair of the workload's matrix on the GPU vs the host; "
+                         "gather: the random-gather calibration along every load path")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.semiring is None:
@@ -744,6 +765,8 @@ def main():
         return run_pack8(args)
     if args.op == "repair":
         return run_repair_compare(args)
+    if args.op == "gather":
+        return run_gather_sweep(args)
     if args.op != "right":
         return run_other_op(args)
 

@@ -39,6 +39,7 @@
 #include <vector>
 
 #include "gmr_internal.h"
+#include "async_copy.cuh"
 #include "device_util.cuh"
 
 namespace gmr {
@@ -2602,12 +2603,17 @@ extern "C" void gmr_pack_free(gmr_pack* p) {
 }
 
 // ------------------------------------------------------------------ gather-bandwidth calibration
-// The sweep's dominant kernel gathers whole 128-byte values at data-dependent
-// addresses; its ceiling is the random-line gather bandwidth of the GPU, from
-// L2 (working set that fits) and from HBM (one that does not).  This
-// calibration measures both with the same access pattern (indices taken
-// modulo the buffer's line count, so every access is in bounds); the
-// sequential mode reads the same lines in order, for the plain read bandwidth.
+// The sweep's dominant kernel gathers whole values (128 bytes at 32 fp32
+// right-hand sides) at data-dependent addresses; its ceiling is the random
+// gather bandwidth of the GPU, from L2 (a working set that fits) and from HBM
+// (one that does not).  This calibration measures it with the same access
+// pattern (unit indices hashed, taken modulo the buffer's unit count, so every
+// access is in bounds) along three load paths:
+//   * lane loads of 16 or 32 bytes, `depth` independent loads in flight per
+//     thread (the sweep's own path; sequential mode reads the units in order);
+//   * one bulk copy per unit into shared memory (cp.async.bulk completing on
+//     an mbarrier), `depth` copies in flight per warp: the path a kernel that
+//     stages values in shared memory would take.
 namespace gmr {
 
 __device__ __forceinline__ unsigned mix32(unsigned x) {
@@ -2619,60 +2625,202 @@ __device__ __forceinline__ unsigned mix32(unsigned x) {
     return x;
 }
 
-__global__ void __launch_bounds__(256) k_gather_lines(const float4* __restrict__ buf, unsigned nlines, int64_t items,
-                                                      bool sequential, float* __restrict__ sink) {
+template <int W>
+__device__ __forceinline__ float lane_load_sum(const unsigned char* p) {
+    if constexpr (W == 16) {
+        const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+        return v.x + v.y + v.z + v.w;
+    } else {
+        float a0, a1, a2, a3, a4, a5, a6, a7;
+        asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                     : "=f"(a0), "=f"(a1), "=f"(a2), "=f"(a3), "=f"(a4), "=f"(a5), "=f"(a6), "=f"(a7)
+                     : "l"(p));
+        return ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+    }
+}
+
+// items units of (W << ushift) bytes; lane access ii reads part ii & (2^ushift - 1)
+// of unit ii >> ushift.  DEPTH accesses per thread are issued before any is used.
+template <int DEPTH, int W>
+__global__ void __launch_bounds__(256) k_gather_units(const unsigned char* __restrict__ buf, unsigned nunits,
+                                                      int ushift, int64_t items, bool sequential,
+                                                      float* __restrict__ sink) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t total = items << ushift;
+    const int64_t unit_bytes = (int64_t)W << ushift;
+    const int64_t part_mask = ((int64_t)1 << ushift) - 1;
     float acc = 0.0f;
-    for (int64_t i = t; i < items * 8; i += 4 * stride) {
-        float4 v[4];
+    for (int64_t i = t; i < total; i += DEPTH * stride) {
+        float v[DEPTH];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
+        for (int j = 0; j < DEPTH; ++j) {
             const int64_t ii = i + j * stride;
-            const unsigned li = (unsigned)(ii >> 3);
-            const unsigned line = (sequential ? li : mix32(li)) % nlines;
-            v[j] = ii < items * 8 ? __ldg(buf + (int64_t)line * 8 + (ii & 7)) : make_float4(0.f, 0.f, 0.f, 0.f);
+            const unsigned ui = (unsigned)(ii >> ushift);
+            const unsigned unit = (sequential ? ui : mix32(ui)) % nunits;
+            v[j] = ii < total ? lane_load_sum<W>(buf + (int64_t)unit * unit_bytes + (ii & part_mask) * W) : 0.0f;
         }
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc += v[j].x + v[j].y + v[j].z + v[j].w;
+        for (int j = 0; j < DEPTH; ++j) acc += v[j];
     }
     if (acc == 1.2345f) sink[t & 255] = acc;  // keeps the loads
 }
 
+static constexpr int kBulkMaxStages = 32;
+
+// Four warps per block; warp w of the grid gathers units gw, gw + nw, ...
+// through its own ring of `stages` shared-memory buffers, one bulk copy per
+// unit issued by lane 0 and consumed (summed) by the whole warp.  A wait that
+// gives up sets *err, drains the warp's copies still in flight (bounded) and
+// returns.
+__global__ void __launch_bounds__(128) k_gather_bulk(const unsigned char* __restrict__ buf, unsigned nunits,
+                                                     int unit_bytes, int stages, int64_t items,
+                                                     unsigned long long spin_limit, float* __restrict__ sink,
+                                                     int* __restrict__ err) {
+    extern __shared__ __align__(128) unsigned char ring_all[];
+    __shared__ __align__(8) uint64_t bar[4][kBulkMaxStages];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char* ring = ring_all + (size_t)warp * stages * unit_bytes;
+    const int64_t gw = (int64_t)blockIdx.x * 4 + warp, nw = (int64_t)gridDim.x * 4;
+    const int64_t mine = gw < items ? (items - gw + nw - 1) / nw : 0;
+    if (lane == 0) {
+        for (int s = 0; s < stages; ++s) mbar_init(&bar[warp][s], 1);
+        mbar_init_fence();
+    }
+    __syncwarp();
+    auto issue = [&](int64_t k) {
+        const int s = (int)(k % stages);
+        const unsigned unit = mix32((unsigned)(gw + k * nw)) % nunits;
+        mbar_arrive_expect_tx(&bar[warp][s], (uint32_t)unit_bytes);
+        bulk_g2s(ring + (size_t)s * unit_bytes, buf + (int64_t)unit * unit_bytes, (uint32_t)unit_bytes,
+                 &bar[warp][s]);
+    };
+    int64_t issued = mine < stages ? mine : stages;
+    if (lane == 0)
+        for (int64_t k = 0; k < issued; ++k) issue(k);
+    float acc = 0.0f;
+    for (int64_t k = 0; k < mine; ++k) {
+        const int s = (int)(k % stages);
+        const uint32_t parity = (uint32_t)((k / stages) & 1);
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(&bar[warp][s], parity, spin_limit));
+        if (!ok) {
+            if (lane == 0) {
+                atomicExch(err, 1);
+                for (int64_t j = k; j < issued; ++j)
+                    mbar_wait(&bar[warp][j % stages], (uint32_t)((j / stages) & 1), spin_limit);
+            }
+            __syncwarp();
+            return;
+        }
+        const float4* p = reinterpret_cast<const float4*>(ring + (size_t)s * unit_bytes);
+        for (int q = lane; q < unit_bytes / 16; q += 32) {
+            const float4 v = p[q];
+            acc += v.x + v.y + v.z + v.w;
+        }
+        __syncwarp();
+        if (k + stages < mine) {
+            if (lane == 0) {
+                fence_proxy_async_smem();
+                issue(k + stages);
+            }
+            ++issued;
+        }
+    }
+    if (acc == 1.2345f) sink[(blockIdx.x * 128 + threadIdx.x) & 255] = acc;
+}
+
+template <int W>
+static void launch_gather_units(int depth, int sms, const unsigned char* buf, unsigned nunits, int ushift,
+                                int64_t items, bool seq, float* sink) {
+    auto go = [&](auto kernel) {
+        int per_sm = 0;
+        GMR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0));
+        kernel<<<std::max(1, per_sm) * sms, 256>>>(buf, nunits, ushift, items, seq, sink);
+    };
+    switch (depth) {
+        case 1: go(k_gather_units<1, W>); break;
+        case 2: go(k_gather_units<2, W>); break;
+        case 4: go(k_gather_units<4, W>); break;
+        case 8: go(k_gather_units<8, W>); break;
+        default: go(k_gather_units<16, W>); break;
+    }
+}
+
 }  // namespace gmr
 
-extern "C" int gmr_measure_gather_bandwidth(int device, int64_t buffer_bytes, int sequential, float* gbs) {
+extern "C" int gmr_measure_gather(int device, int64_t buffer_bytes, int mode, int depth, int unit_bytes,
+                                  float* gbs) {
     return guarded([&] {
-        if (!gbs || buffer_bytes < 4096 || buffer_bytes > (int64_t)64 << 30) throw Error(GMR_ERR_ARG, "bad argument");
+        if (!gbs || buffer_bytes < 4096 || buffer_bytes > (int64_t)64 << 30) throw Error(GMR_ERR_ARG, "bad buffer size");
+        if (mode < GMR_GATHER_LOAD16 || mode > GMR_GATHER_BULK) throw Error(GMR_ERR_ARG, "unknown gather mode");
+        if (unit_bytes < 16 || (unit_bytes & (unit_bytes - 1)) || unit_bytes > 16384)
+            throw Error(GMR_ERR_ARG, "unit_bytes must be a power of two in [16, 16384]");
+        const bool bulk = mode == GMR_GATHER_BULK;
+        const int W = mode == GMR_GATHER_LOAD32 ? 32 : 16;
+        if (!bulk && (depth != 1 && depth != 2 && depth != 4 && depth != 8 && depth != 16))
+            throw Error(GMR_ERR_ARG, "depth must be 1, 2, 4, 8 or 16 loads per thread");
+        if (!bulk && unit_bytes < W) throw Error(GMR_ERR_ARG, "unit smaller than one lane access");
+        if (bulk && (depth < 1 || depth > kBulkMaxStages)) throw Error(GMR_ERR_ARG, "depth must be 1..32 stages");
+        const size_t smem = bulk ? (size_t)4 * depth * unit_bytes : 0;
+        if (smem > (size_t)200 * 1024) throw Error(GMR_ERR_RANGE, "4 warps x depth x unit_bytes beyond 200 KB");
         DeviceGuard dg(device);
-        const int64_t lines = buffer_bytes / 128;
-        DevBuf buf, sink;
-        buf.ensure((size_t)lines * 128);
+        const int64_t units = buffer_bytes / unit_bytes;
+        if (units < 1 || units > 0xffffffffLL) throw Error(GMR_ERR_ARG, "bad unit count");
+        DevBuf buf, sink, errb;
+        buf.ensure((size_t)units * unit_bytes);
         sink.ensure(1024);
-        GMR_CUDA(cudaMemset(buf.p, 0, (size_t)lines * 128));
+        errb.ensure(16);
+        GMR_CUDA(cudaMemset(buf.p, 0, (size_t)units * unit_bytes));
+        GMR_CUDA(cudaMemset(errb.p, 0, 16));
         int sms = 152;
         GMR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-        const int64_t items = 50000000;  // 128-byte lines gathered per timed run
-        cudaEvent_t a, b;
+        const int64_t items = std::max<int64_t>(1, ((int64_t)6400 << 20) / unit_bytes);  // ~6.7 GB per timed run
+        int ushift = 0;
+        while ((W << ushift) < unit_bytes) ++ushift;
+        const unsigned char* b = static_cast<const unsigned char*>(buf.p);
+        float* sk = static_cast<float*>(sink.p);
+        int* er = static_cast<int*>(errb.p);
+        int bulk_blocks = 0;
+        if (bulk) {
+            GMR_CUDA(cudaFuncSetAttribute(k_gather_bulk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            GMR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bulk_blocks, k_gather_bulk, 128, smem));
+            if (bulk_blocks < 1) throw Error(GMR_ERR_RANGE, "bulk gather kernel cannot be resident");
+            bulk_blocks *= sms;
+        }
+        auto run = [&](int64_t n) {
+            if (bulk)
+                k_gather_bulk<<<bulk_blocks, 128, smem>>>(b, (unsigned)units, unit_bytes, depth, n, 20000000ull, sk,
+                                                           er);
+            else if (W == 32)
+                launch_gather_units<32>(depth, sms, b, (unsigned)units, ushift, n, mode == GMR_GATHER_SEQ16, sk);
+            else
+                launch_gather_units<16>(depth, sms, b, (unsigned)units, ushift, n, mode == GMR_GATHER_SEQ16, sk);
+        };
+        cudaEvent_t a, e;
         GMR_CUDA(cudaEventCreate(&a));
-        GMR_CUDA(cudaEventCreate(&b));
-        k_gather_lines<<<sms * 16, 256>>>(static_cast<const float4*>(buf.p), (unsigned)lines, items / 10,
-                                          sequential != 0, static_cast<float*>(sink.p));
+        GMR_CUDA(cudaEventCreate(&e));
+        run(items / 10);
         float best = 0.0f;
         for (int r = 0; r < 3; ++r) {
             cudaEventRecord(a);
-            k_gather_lines<<<sms * 16, 256>>>(static_cast<const float4*>(buf.p), (unsigned)lines, items,
-                                              sequential != 0, static_cast<float*>(sink.p));
-            cudaEventRecord(b);
-            GMR_CUDA(cudaEventSynchronize(b));
+            run(items);
+            cudaEventRecord(e);
+            GMR_CUDA(cudaEventSynchronize(e));
             float ms = 0.0f;
-            cudaEventElapsedTime(&ms, a, b);
-            best = std::max(best, (float)(items * 128.0 / (ms * 1e6)));
+            cudaEventElapsedTime(&ms, a, e);
+            best = std::max(best, (float)((double)items * unit_bytes / (ms * 1e6)));
         }
         cudaEventDestroy(a);
-        cudaEventDestroy(b);
+        cudaEventDestroy(e);
         GMR_CUDA(cudaGetLastError());
+        int failed = 0;
+        GMR_CUDA(cudaMemcpy(&failed, er, sizeof(int), cudaMemcpyDeviceToHost));
+        if (failed) throw Error(GMR_ERR_TIMEOUT, "a bulk-copy wait gave up");
         *gbs = best;
     });
+}
+
+extern "C" int gmr_measure_gather_bandwidth(int device, int64_t buffer_bytes, int sequential, float* gbs) {
+    return gmr_measure_gather(device, buffer_bytes, sequential ? GMR_GATHER_SEQ16 : GMR_GATHER_LOAD16, 4, 128, gbs);
 }
 
 // ------------------------------------------------------------------ no-allocation entry point

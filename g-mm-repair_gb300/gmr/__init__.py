@@ -583,6 +583,21 @@ def measure_gather_bandwidth(buffer_bytes: int, device: int = 0, sequential: boo
     return float(g.value)
 
 
+GATHER_MODES = {"load16": 0, "seq16": 1, "load32": 2, "bulk": 3}
+
+
+def measure_gather(buffer_bytes: int, mode: str = "load16", depth: int = 4, unit_bytes: int = 128,
+                   device: int = 0) -> float:
+    """Gather bandwidth (GB/s) of random units of unit_bytes over a buffer of
+    that size along one load path: "load16" / "load32" lane loads with `depth`
+    loads in flight per thread, "seq16" the same in order, "bulk" one bulk copy
+    per unit into shared memory with `depth` copies in flight per warp."""
+    g = C.c_float()
+    _check(lib().gmr_measure_gather(device, int(buffer_bytes), GATHER_MODES[mode], int(depth), int(unit_bytes),
+                                    C.byref(g)))
+    return float(g.value)
+
+
 # ---------------------------------------------------------------- legacy ABI
 def _legacy_args(rows, cols, alpha, rules_lrc, val_indices, col_indices, V, sched):
     keep = []

@@ -120,6 +120,7 @@ _SIGS = {
     "gmr_engine_autotune": (C.c_int, [P, C.c_int, P, P, C.c_int, P, C.c_int, F32P, C.c_int]),
     "gmr_engine_autotune_energy": (C.c_int, [P, C.c_int, P, P, C.c_int, P, C.c_int, C.c_float, F32P, C.c_int]),
     "gmr_measure_gather_bandwidth": (C.c_int, [C.c_int, C.c_int64, C.c_int, F32P]),
+    "gmr_measure_gather": (C.c_int, [C.c_int, C.c_int64, C.c_int, C.c_int, C.c_int, F32P]),
     "gmr_engine_status": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "gmr_engine_last_launches": (C.c_int64, [P]),
     "gmr_plan_prepare_left": (C.c_int, [P]),

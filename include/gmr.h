@@ -372,6 +372,20 @@ int gmr_engine_choose_learned(gmr_engine* e, const gmr_plan* p, const gmr_mlp* m
  * sequential != 0 reads the lines in order instead (plain read bandwidth).
  * Allocates the buffer for the measurement. */
 int gmr_measure_gather_bandwidth(int device, int64_t buffer_bytes, int sequential, float* gbs);
+/* The same calibration along the load paths a kernel can take (GB/s of units
+ * gathered; the buffer is allocated for the measurement):
+ *  GMR_GATHER_LOAD16 / GMR_GATHER_LOAD32: random units of unit_bytes read with
+ *    16- / 32-byte lane loads, `depth` (1, 2, 4, 8, 16) loads in flight per
+ *    thread before any is used;
+ *  GMR_GATHER_SEQ16: the same 16-byte loads over the units in order;
+ *  GMR_GATHER_BULK: one bulk copy (cp.async.bulk, completing on an mbarrier)
+ *    per random unit into shared memory, `depth` (1..32) copies in flight per
+ *    warp, 4 warps per block; 4 * depth * unit_bytes <= 200 KB.
+ * unit_bytes: a power of two in [16, 16384] (at least one lane access).
+ * gmr_measure_gather_bandwidth is GMR_GATHER_LOAD16 (or SEQ16), depth 4,
+ * 128-byte units.  GMR_ERR_TIMEOUT if a bulk-copy wait gave up. */
+enum { GMR_GATHER_LOAD16 = 0, GMR_GATHER_SEQ16 = 1, GMR_GATHER_LOAD32 = 2, GMR_GATHER_BULK = 3 };
+int gmr_measure_gather(int device, int64_t buffer_bytes, int mode, int depth, int unit_bytes, float* gbs);
 
 /* Status of the engine's last GMR_VARIANT_PERSISTENT multiply, valid once the
  * stream it ran on has been synchronized: *failed != 0 when a grid-barrier

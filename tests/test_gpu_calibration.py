@@ -16,3 +16,22 @@ def test_gather_bandwidth_l2_above_hbm():
 def test_gather_bandwidth_rejects_bad_size():
     with pytest.raises(gmr.GmrError):
         gmr.measure_gather_bandwidth(16)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode,depth,unit", [("load16", 8, 128), ("load32", 4, 128), ("seq16", 16, 128),
+                                             ("bulk", 8, 128), ("bulk", 2, 4096)])
+def test_gather_load_paths(mode, depth, unit):
+    """Every load path of the calibration runs to completion (bulk copies:
+    every mbarrier wait completes) and gives a rate inside physical bounds."""
+    gbs = gmr.measure_gather(32 << 20, mode=mode, depth=depth, unit_bytes=unit)
+    assert 100.0 < gbs < 50000.0
+
+
+@pytest.mark.parametrize("kw", [dict(mode="bulk", depth=33), dict(mode="load16", depth=3),
+                                dict(mode="load32", unit_bytes=16), dict(mode="bulk", depth=32, unit_bytes=4096),
+                                dict(unit_bytes=96)])
+def test_gather_rejects_bad_arguments(kw):
+    """Checked on the host before any device work."""
+    with pytest.raises(gmr.GmrError):
+        gmr.measure_gather(32 << 20, **kw)
