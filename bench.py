@@ -48,6 +48,8 @@ MOSAICS = {
     "mosaic-20000x5000": (20_000, 5_000, 64, 0.01, 1e-3, 0),
 }
 GRAPH = (16_777_216, 24, 0.7, 3)  # nodes, mean out-degree, copy probability, seed
+# bytes each lane moves per value access: the engine's default, or GMR_LANE_BYTES
+LANE_BYTES = os.environ.get("GMR_LANE_BYTES", "default: 32 for (+,x) tiles of >= 32 words, else 16")
 WORKLOADS = list(MOSAICS) + ["graph-16777216", "pack8"]
 SR_IDS = {"plustimes": 0, "boolean": 1, "tropical": 2}
 INT_MAX = 2**31 - 1
@@ -431,6 +433,7 @@ VARIANT_NAMES = {0: "auto (learned per-launch table, CUDA graph)", 1: "plain", 2
 def run_config(args, rows, cols, ws):
     """The line's config: the same keys on both arms."""
     return workload_config(args, rows, cols) | {"variant": VARIANT_NAMES[args.variant],
+                                                "lane_bytes": LANE_BYTES,
                                                 "parallelism": f"replicas x{ws}"}
 
 
@@ -712,7 +715,7 @@ def run_gather_sweep(args):
     import gmr
 
     cases = ([("load16", d, 128) for d in (1, 2, 4, 8, 16)] + [("load32", d, 128) for d in (2, 4, 8)] +
-             [("seq16", d, 128) for d in (4, 16)] + [("bulk", d, 128) for d in (2, 4, 8, 16, 32)] +
+             [("seq16", d, 128) for d in (4, 16)] + [("bulk", d, 128) for d in (2, 8, 16, 32, 64)] +
              [("bulk", 4, u) for u in (512, 2048, 8192)])
     rows = []
     for buf in (64 << 20, 4 << 30):
@@ -852,6 +855,9 @@ def main():
         tuning["default_vps"] = B * 1000.0 / timed(20, variant=3)
         tuning["default_pull_vps"] = B * 1000.0 / timed(20, variant=3, push=1)
         tuning["default_push_vps"] = B * 1000.0 / timed(20, variant=3, push=2)
+        # the same untuned multiply with 16- and 32-byte lane accesses, back to back
+        tuning["default_lane16_vps"] = B * 1000.0 / timed(20, variant=3, lane_bytes=16)
+        tuning["default_lane32_vps"] = B * 1000.0 / timed(20, variant=3, lane_bytes=32)
         if not args.no_tune:
             t0 = time.perf_counter()
             eng.autotune(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, reps=3)

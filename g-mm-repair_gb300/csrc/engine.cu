@@ -83,10 +83,34 @@ struct alignas(sizeof(T) * N) Vec {
     T v[N];
 };
 
+// 32-byte accesses (8 words per lane): one 256-bit load or store per lane.
+// Volatile asm keeps each access where the program places it (in particular
+// on its side of a grid barrier in the persistent sweep).
+#define GMR_V8_OUT(u) "=r"(u[0]), "=r"(u[1]), "=r"(u[2]), "=r"(u[3]), "=r"(u[4]), "=r"(u[5]), "=r"(u[6]), "=r"(u[7])
+template <int MODE>  // 0 read-only path (.nc), 1 plain, 2 L2 only (.cg)
+__device__ __forceinline__ void ld_v8(const void* p, uint32_t (&u)[8]) {
+    if constexpr (MODE == 0)
+        asm volatile("ld.global.nc.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];" : GMR_V8_OUT(u) : "l"(p));
+    else if constexpr (MODE == 1)
+        asm volatile("ld.global.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];" : GMR_V8_OUT(u) : "l"(p) : "memory");
+    else
+        asm volatile("ld.global.cg.v8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];" : GMR_V8_OUT(u) : "l"(p) : "memory");
+}
+#undef GMR_V8_OUT
+__device__ __forceinline__ void st_v8(void* p, const uint32_t (&u)[8]) {
+    asm volatile("st.global.v8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "r"(u[0]), "r"(u[1]), "r"(u[2]),
+                 "r"(u[3]), "r"(u[4]), "r"(u[5]), "r"(u[6]), "r"(u[7])
+                 : "memory");
+}
+
 template <class T, int N>
 __device__ __forceinline__ Vec<T, N> vload(const T* p) {
     Vec<T, N> r;
-    if constexpr (N == 4) {
+    if constexpr (N == 8) {
+        uint32_t u[8];
+        ld_v8<0>(p, u);
+        memcpy(&r, u, 32);
+    } else if constexpr (N == 4) {
         uint4 u = __ldg(reinterpret_cast<const uint4*>(p));
         memcpy(&r, &u, 16);
     } else if constexpr (N == 2) {
@@ -103,7 +127,13 @@ __device__ __forceinline__ Vec<T, N> vload(const T* p) {
 // where a line left in this SM's L1 could be stale.
 template <class T, int N, bool CG = false>
 __device__ __forceinline__ Vec<T, N> vload_rw(const T* p) {
-    if constexpr (CG) {
+    if constexpr (N == 8) {
+        Vec<T, N> r;
+        uint32_t u[8];
+        ld_v8<CG ? 2 : 1>(p, u);
+        memcpy(&r, u, 32);
+        return r;
+    } else if constexpr (CG) {
         Vec<T, N> r;
         if constexpr (N == 4) {
             uint4 u = __ldcg(reinterpret_cast<const uint4*>(p));
@@ -122,7 +152,13 @@ __device__ __forceinline__ Vec<T, N> vload_rw(const T* p) {
 }
 template <class T, int N>
 __device__ __forceinline__ void vstore(T* p, const Vec<T, N>& v) {
-    *reinterpret_cast<Vec<T, N>*>(p) = v;
+    if constexpr (N == 8) {
+        uint32_t u[8];
+        memcpy(u, &v, 32);
+        st_v8(p, u);
+    } else {
+        *reinterpret_cast<Vec<T, N>*>(p) = v;
+    }
 }
 
 template <class S, int N>
@@ -142,7 +178,10 @@ __device__ __forceinline__ Vec<typename S::T, N> vzero() {
 }
 template <class S, int N>
 __device__ __forceinline__ void vred(typename S::T* p, const Vec<typename S::T, N>& v) {
-    if constexpr (std::is_same<S, SPlus>::value && N == 4) {
+    if constexpr (std::is_same<S, SPlus>::value && N == 8) {
+        atomicAdd(reinterpret_cast<float4*>(p), make_float4(v.v[0], v.v[1], v.v[2], v.v[3]));
+        atomicAdd(reinterpret_cast<float4*>(p + 4), make_float4(v.v[4], v.v[5], v.v[6], v.v[7]));
+    } else if constexpr (std::is_same<S, SPlus>::value && N == 4) {
         atomicAdd(reinterpret_cast<float4*>(p), make_float4(v.v[0], v.v[1], v.v[2], v.v[3]));
     } else if constexpr (std::is_same<S, SPlus>::value && N == 2) {
         atomicAdd(reinterpret_cast<float2*>(p), make_float2(v.v[0], v.v[1]));
@@ -552,7 +591,7 @@ __device__ __forceinline__ void emits_t(const SweepArgs& a, const LevelArgs& L, 
 // DIRK (direct terminals): 0 off; 1 rule children are terminal codes; 2 the
 // emissions too (the launch that folds the terminal emissions).
 template <class S, int VEC, int GLOG, int EMIT, int DIRK = 0>
-__global__ void __launch_bounds__(256) k_level(SweepArgs a, LevelArgs L) {
+__global__ void __launch_bounds__(256, VEC == 8 ? 4 : 1) k_level(SweepArgs a, LevelArgs L) {
     const int tile = a.t0 + blockIdx.y;
     if ((int)blockIdx.x < L.em_blocks) {
         const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -827,6 +866,7 @@ struct gmr_engine {
     gmr::DevBuf em_tcode, rule_terms, ops_direct;
     int64_t n_rule_terms = 0;
     bool direct_terms = false;
+    int lane_bytes = 0;  // bytes per lane access when gmr_config::lane_bytes = 0 (0: by semiring and tile); GMR_LANE_BYTES
     // Push lists (LevelArgs::pe_off): the emissions of levels 1..depth ordered
     // by source slot, rows ascending per slot; push_ok[k] = every emission of
     // level k has a slot of level k as its source, so level k can push.
@@ -1191,6 +1231,17 @@ static void launch_persistent_s(gmr_engine* e, const Launch& lc, const void* X, 
             default: return launch_persistent_t<S, 4, -1>(e, lc, X, Y, st, n);
         }
     }
+    if constexpr (!std::is_same<S, SBool>::value) {
+        if (lc.VEC == 8) {
+            switch (lc.G) {
+                case 1: return launch_persistent_t<S, 8, 0>(e, lc, X, Y, st, n);
+                case 2: return launch_persistent_t<S, 8, 1>(e, lc, X, Y, st, n);
+                case 4: return launch_persistent_t<S, 8, 2>(e, lc, X, Y, st, n);
+                case 8: return launch_persistent_t<S, 8, 3>(e, lc, X, Y, st, n);
+                default: return launch_persistent_t<S, 8, 4>(e, lc, X, Y, st, n);
+            }
+        }
+    }
     if (lc.VEC == 2 && lc.G == 1) return launch_persistent_t<S, 2, 0>(e, lc, X, Y, st, n);
     if (lc.VEC == 1 && lc.G == 1) return launch_persistent_t<S, 1, 0>(e, lc, X, Y, st, n);
     if (lc.VEC == 2) return launch_persistent_t<S, 2, -1>(e, lc, X, Y, st, n);
@@ -1218,6 +1269,17 @@ static void launch_chain_s(gmr_engine* e, const Launch& lc, const void* X, void*
             default: return launch_chain_t<S, 4, -1>(e, lc, X, Y, st, n);
         }
     }
+    if constexpr (!std::is_same<S, SBool>::value) {
+        if (lc.VEC == 8) {
+            switch (lc.G) {
+                case 1: return launch_chain_t<S, 8, 0>(e, lc, X, Y, st, n);
+                case 2: return launch_chain_t<S, 8, 1>(e, lc, X, Y, st, n);
+                case 4: return launch_chain_t<S, 8, 2>(e, lc, X, Y, st, n);
+                case 8: return launch_chain_t<S, 8, 3>(e, lc, X, Y, st, n);
+                default: return launch_chain_t<S, 8, 4>(e, lc, X, Y, st, n);
+            }
+        }
+    }
     if (lc.VEC == 2 && lc.G == 1) return launch_chain_t<S, 2, 0>(e, lc, X, Y, st, n);
     if (lc.VEC == 1 && lc.G == 1) return launch_chain_t<S, 1, 0>(e, lc, X, Y, st, n);
     if (lc.VEC == 2) return launch_chain_t<S, 2, -1>(e, lc, X, Y, st, n);
@@ -1239,7 +1301,10 @@ static int auto_tile(gmr_engine*, int Bw) {
     return bt;
 }
 
-static Launch resolve_launch(gmr_engine* e, int semiring, int B, const void* X, void* Y, const gmr_config* cfg) {
+// max_vec: the widest lane access a caller's kernels instantiate (the pack
+// and the left product stop at 4 words).
+static Launch resolve_launch(gmr_engine* e, int semiring, int B, const void* X, void* Y, const gmr_config* cfg,
+                             int max_vec = 8) {
     Launch lc{};
     lc.semiring = semiring;
     lc.B = B;
@@ -1273,7 +1338,16 @@ static Launch resolve_launch(gmr_engine* e, int semiring, int B, const void* X, 
         lc.tile_levels = std::max(K, 1);
     }
     auto aligned = [&](size_t al) { return ((uintptr_t)X % al == 0) && ((uintptr_t)Y % al == 0); };
-    if (lc.Bt % 4 == 0 && lc.Bw % 4 == 0 && aligned(16)) lc.VEC = 4;
+    int lane_bytes = cfg && cfg->lane_bytes ? cfg->lane_bytes : e->lane_bytes;
+    if (lane_bytes != 0 && lane_bytes != 16 && lane_bytes != 32) throw Error(GMR_ERR_ARG, "lane_bytes must be 0, 16 or 32");
+    // 8 words per lane: fp32 / int32 tiles of 8..128 words (powers of two), 32-byte aligned X and Y
+    const bool v8_ok = max_vec >= 8 && semiring != GMR_BOOLEAN && lc.Bt % 8 == 0 && lc.Bw % 8 == 0 &&
+                       lc.Bt <= 128 && (lc.Bt & (lc.Bt - 1)) == 0 && aligned(32);
+    // measured on the 200k x 10k grammar: 32-byte lanes win for (+,x) tiles of
+    // >= 32 words (B = 32 / 64 / 128), lose at 8 words and for (min,+)
+    if (lane_bytes == 0) lane_bytes = semiring == GMR_PLUS_TIMES && lc.Bt >= 32 ? 32 : 16;
+    if (lane_bytes == 32 && v8_ok) lc.VEC = 8;
+    else if (lc.Bt % 4 == 0 && lc.Bw % 4 == 0 && aligned(16)) lc.VEC = 4;
     else if (lc.Bt % 2 == 0 && lc.Bw % 2 == 0 && aligned(8)) lc.VEC = 2;
     else lc.VEC = 1;
     lc.G = lc.Bt / lc.VEC;
@@ -1536,6 +1610,10 @@ extern "C" int gmr_engine_create(const gmr_plan* p, int device, gmr_engine** out
             upload(p->term_col, e->term_col);
             upload(p->V, e->V);
             build_direct_terms(*p, *e);
+            if (const char* f = std::getenv("GMR_LANE_BYTES")) {
+                const int lb = std::atoi(f);
+                if (lb == 16 || lb == 32) e->lane_bytes = lb;
+            }
             build_push_lists(*p, *e);
             GMR_CUDA(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking));
             GMR_CUDA(cudaDeviceGetAttribute(&e->sm_count, cudaDevAttrMultiProcessorCount, device));
@@ -2507,7 +2585,7 @@ extern "C" int gmr_pack_multiply(gmr_pack* p, const int* semirings, const void* 
             if (semirings[i] < 0 || semirings[i] > 2) throw Error(GMR_ERR_ARG, "unknown semiring");
             if (B[i] < 1) throw Error(GMR_ERR_ARG, "B must be >= 1");
             if (((uintptr_t)dX[i] | (uintptr_t)dY[i]) % 4 != 0) throw Error(GMR_ERR_ARG, "misaligned X or Y");
-            Launch lc = resolve_launch(e, semirings[i], B[i], dX[i], dY[i], nullptr);
+            Launch lc = resolve_launch(e, semirings[i], B[i], dX[i], dY[i], nullptr, 4);
             ensure_scratch(e, lc.Bw);
             lcs.push_back(lc);
         }
@@ -2665,63 +2743,74 @@ __global__ void __launch_bounds__(256) k_gather_units(const unsigned char* __res
     if (acc == 1.2345f) sink[t & 255] = acc;  // keeps the loads
 }
 
-static constexpr int kBulkMaxStages = 32;
+static constexpr int kBulkMaxDepth = 64;
 
 // Four warps per block; warp w of the grid gathers units gw, gw + nw, ...
-// through its own ring of `stages` shared-memory buffers, one bulk copy per
-// unit issued by lane 0 and consumed (summed) by the whole warp.  A wait that
+// through two shared-memory stages of depth/2 units each.  One barrier phase
+// covers a whole stage: lane 0 posts the stage's byte count, then lane j
+// issues the bulk copy of the stage's unit j, so depth copies are in flight
+// per warp and the barrier work is paid once per depth/2 copies.  A wait that
 // gives up sets *err, drains the warp's copies still in flight (bounded) and
 // returns.
 __global__ void __launch_bounds__(128) k_gather_bulk(const unsigned char* __restrict__ buf, unsigned nunits,
-                                                     int unit_bytes, int stages, int64_t items,
+                                                     int unit_bytes, int depth, int64_t items,
                                                      unsigned long long spin_limit, float* __restrict__ sink,
                                                      int* __restrict__ err) {
     extern __shared__ __align__(128) unsigned char ring_all[];
-    __shared__ __align__(8) uint64_t bar[4][kBulkMaxStages];
+    __shared__ __align__(8) uint64_t bar[4][2];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char* ring = ring_all + (size_t)warp * stages * unit_bytes;
+    const int per = depth / 2;
+    unsigned char* ring = ring_all + (size_t)warp * depth * unit_bytes;
     const int64_t gw = (int64_t)blockIdx.x * 4 + warp, nw = (int64_t)gridDim.x * 4;
     const int64_t mine = gw < items ? (items - gw + nw - 1) / nw : 0;
+    const int64_t groups = (mine + per - 1) / per;
     if (lane == 0) {
-        for (int s = 0; s < stages; ++s) mbar_init(&bar[warp][s], 1);
+        mbar_init(&bar[warp][0], 1);
+        mbar_init(&bar[warp][1], 1);
         mbar_init_fence();
     }
     __syncwarp();
-    auto issue = [&](int64_t k) {
-        const int s = (int)(k % stages);
-        const unsigned unit = mix32((unsigned)(gw + k * nw)) % nunits;
-        mbar_arrive_expect_tx(&bar[warp][s], (uint32_t)unit_bytes);
-        bulk_g2s(ring + (size_t)s * unit_bytes, buf + (int64_t)unit * unit_bytes, (uint32_t)unit_bytes,
-                 &bar[warp][s]);
+    auto issue = [&](int64_t g) {  // called by the whole warp
+        const int s = (int)(g & 1);
+        const int64_t k0 = g * per;
+        const int n = (int)min((int64_t)per, mine - k0);
+        if (lane == 0) mbar_arrive_expect_tx(&bar[warp][s], (uint32_t)(n * unit_bytes));
+        __syncwarp();
+        if (lane < n) {
+            const unsigned unit = mix32((unsigned)(gw + (k0 + lane) * nw)) % nunits;
+            bulk_g2s(ring + ((size_t)s * per + lane) * unit_bytes, buf + (int64_t)unit * unit_bytes,
+                     (uint32_t)unit_bytes, &bar[warp][s]);
+        }
     };
-    int64_t issued = mine < stages ? mine : stages;
-    if (lane == 0)
-        for (int64_t k = 0; k < issued; ++k) issue(k);
+    int64_t issued = groups < 2 ? groups : 2;
+    for (int64_t g = 0; g < issued; ++g) issue(g);
     float acc = 0.0f;
-    for (int64_t k = 0; k < mine; ++k) {
-        const int s = (int)(k % stages);
-        const uint32_t parity = (uint32_t)((k / stages) & 1);
-        const bool ok = __all_sync(0xffffffffu, mbar_wait(&bar[warp][s], parity, spin_limit));
+    for (int64_t g = 0; g < groups; ++g) {
+        const int s = (int)(g & 1);
+        const uint32_t parity = (uint32_t)((g >> 1) & 1);
+        // lane 0 polls; __syncwarp then orders the other lanes' reads after
+        // its observation of the completed phase
+        int ok = 1;
+        if (lane == 0) ok = mbar_wait(&bar[warp][s], parity, spin_limit) ? 1 : 0;
+        __syncwarp();
+        ok = __shfl_sync(0xffffffffu, ok, 0);
         if (!ok) {
             if (lane == 0) {
                 atomicExch(err, 1);
-                for (int64_t j = k; j < issued; ++j)
-                    mbar_wait(&bar[warp][j % stages], (uint32_t)((j / stages) & 1), spin_limit);
+                for (int64_t j = g; j < issued; ++j) mbar_wait(&bar[warp][j & 1], (uint32_t)((j >> 1) & 1), spin_limit);
             }
             __syncwarp();
             return;
         }
-        const float4* p = reinterpret_cast<const float4*>(ring + (size_t)s * unit_bytes);
-        for (int q = lane; q < unit_bytes / 16; q += 32) {
+        const int n = (int)min((int64_t)per, mine - g * per);
+        const float4* p = reinterpret_cast<const float4*>(ring + (size_t)s * per * unit_bytes);
+        for (int q = lane; q < n * unit_bytes / 16; q += 32) {
             const float4 v = p[q];
             acc += v.x + v.y + v.z + v.w;
         }
-        __syncwarp();
-        if (k + stages < mine) {
-            if (lane == 0) {
-                fence_proxy_async_smem();
-                issue(k + stages);
-            }
+        __syncwarp();  // every lane's reads of stage s have returned (they fed acc)
+        if (g + 2 < groups) {
+            issue(g + 2);
             ++issued;
         }
     }
@@ -2759,7 +2848,7 @@ extern "C" int gmr_measure_gather(int device, int64_t buffer_bytes, int mode, in
         if (!bulk && (depth != 1 && depth != 2 && depth != 4 && depth != 8 && depth != 16))
             throw Error(GMR_ERR_ARG, "depth must be 1, 2, 4, 8 or 16 loads per thread");
         if (!bulk && unit_bytes < W) throw Error(GMR_ERR_ARG, "unit smaller than one lane access");
-        if (bulk && (depth < 1 || depth > kBulkMaxStages)) throw Error(GMR_ERR_ARG, "depth must be 1..32 stages");
+        if (bulk && (depth < 2 || depth > kBulkMaxDepth || depth % 2)) throw Error(GMR_ERR_ARG, "depth must be even, 2..64 copies");
         const size_t smem = bulk ? (size_t)4 * depth * unit_bytes : 0;
         if (smem > (size_t)200 * 1024) throw Error(GMR_ERR_RANGE, "4 warps x depth x unit_bytes beyond 200 KB");
         DeviceGuard dg(device);

@@ -421,8 +421,8 @@ class Engine:
         self.close()
 
     @staticmethod
-    def _cfg(variant=0, emit_mode=0, ops_per_cta=0, vec_tile=0, tile_levels=0, spin_limit=0, push=0):
-        return Config(variant, vec_tile, ops_per_cta, emit_mode, tile_levels, spin_limit, push)
+    def _cfg(variant=0, emit_mode=0, ops_per_cta=0, vec_tile=0, tile_levels=0, spin_limit=0, push=0, lane_bytes=0):
+        return Config(variant, vec_tile, ops_per_cta, emit_mode, tile_levels, spin_limit, push, lane_bytes)
 
     def status(self):
         """(failed, phase) of the last persistent multiply (after a stream synchronize)."""

@@ -63,7 +63,7 @@ class DevicePlan(C.Structure):
 
 class Config(C.Structure):
     _fields_ = [("variant", C.c_int), ("vec_tile", C.c_int), ("ops_per_cta", C.c_int), ("emit_mode", C.c_int),
-                ("tile_levels", C.c_int), ("spin_limit", C.c_int), ("push", C.c_int)]
+                ("tile_levels", C.c_int), ("spin_limit", C.c_int), ("push", C.c_int), ("lane_bytes", C.c_int)]
 
 
 P = C.c_void_p

@@ -133,13 +133,16 @@ def choose_learned(eng: Engine, plan: Plan, model: Mlp, semiring, B: int) -> np.
 
 # ---------------------------------------------------------------- corpus
 def corpus_specs(n_mosaic: int, n_graph: int, seed0: int = 100, full: bool = True):
-    """Seeded grammar specs of the scheduler corpus (seeds seed0, seed0+1, ...):
-    mosaics with rows 10k-500k and cols 1k-20k, both log-uniform (rows shrunk
-    so that rows x cols x 1/2 stays below 1.2e9 non-zeros, the size the GPU
-    RePair holds comfortably), founders 16-1024, switch rate 1e-3 to 5e-2;
-    weighted copy-model graphs with 0.2M-16.8M nodes (log-uniform), degree
-    8-32, copy probability 0.3-0.9.  full=False keeps the earlier small ranges
-    (rows 10k-60k, cols 1k-10k, nodes 0.2M-1.5M) for quick runs."""
+    """Seeded grammar specs of the scheduler corpus, one seed per grammar:
+    mosaics take seeds seed0 .. seed0 + n_mosaic - 1, graphs the next n_graph
+    (seed0 = 100 and 192 + 64 grammars give seeds 100-355).  Mosaics: rows
+    10k-500k and cols 1k-20k, both log-uniform, with rows shrunk so that
+    rows x cols x 1/2 stays below 1.2e9 non-zeros (the size the GPU RePair
+    holds comfortably; 500k x 20k would be 5e9), founders 16-1024, switch
+    rate 1e-3 to 5e-2.  Weighted copy-model graphs: 1M-16.8M nodes
+    (log-uniform), degree 8-64, copy probability 0.3-0.9.  full=False keeps
+    small ranges (rows 10k-60k, cols 1k-10k, nodes 0.2M-1.5M, degree 8-32)
+    for quick runs."""
     specs = []
     for i in range(n_mosaic):
         r = np.random.default_rng(seed0 + i)
@@ -152,11 +155,12 @@ def corpus_specs(n_mosaic: int, n_graph: int, seed0: int = 100, full: bool = Tru
         specs.append(dict(kind="mosaic", seed=seed0 + i, rows=rows, cols=cols, founders=int(2 ** r.uniform(4, 10)),
                           switch=float(10 ** r.uniform(-3, np.log10(5e-2))), mutation=1e-3))
     for i in range(n_graph):
-        r = np.random.default_rng(seed0 + 1000 + i)
-        nodes = (int(np.exp(r.uniform(np.log(200_000), np.log(16_777_216)))) if full
+        seed = seed0 + n_mosaic + i
+        r = np.random.default_rng(seed)
+        nodes = (int(np.exp(r.uniform(np.log(1_000_000), np.log(16_777_216)))) if full
                  else int(r.integers(200_000, 1_500_001)))
-        specs.append(dict(kind="graph", seed=seed0 + 1000 + i, nodes=nodes,
-                          degree=int(r.integers(8, 33)), copy=float(r.uniform(0.3, 0.9))))
+        degree = int(r.integers(8, 65)) if full else int(r.integers(8, 33))
+        specs.append(dict(kind="graph", seed=seed, nodes=nodes, degree=degree, copy=float(r.uniform(0.3, 0.9))))
     return specs
 
 

@@ -241,6 +241,13 @@ typedef struct {
                          may take before it gives up (0 = 20,000,000) */
     int push;         /* GMR_PUSH_*: whether rules fold their own values into
                          the rows that emit them (see GMR_LEVEL_PUSH) */
+    int lane_bytes;   /* bytes each lane moves per value access: 16, or 32
+                         (256-bit loads and stores, 8 words per lane; used for
+                         (+,x) and (min,+) when the tile is 8, 16, 32, 64 or
+                         128 words and X and Y are 32-byte aligned, else 16);
+                         0 = engine default: 32 for (+,x) tiles of 32 words
+                         or more, else 16 (GMR_LANE_BYTES=16|32 at engine
+                         creation overrides it) */
 } gmr_config;
 enum {
     GMR_PUSH_AUTO = 0,       /* the installed per-launch table, else the engine's rule */
@@ -378,9 +385,10 @@ int gmr_measure_gather_bandwidth(int device, int64_t buffer_bytes, int sequentia
  *    16- / 32-byte lane loads, `depth` (1, 2, 4, 8, 16) loads in flight per
  *    thread before any is used;
  *  GMR_GATHER_SEQ16: the same 16-byte loads over the units in order;
- *  GMR_GATHER_BULK: one bulk copy (cp.async.bulk, completing on an mbarrier)
- *    per random unit into shared memory, `depth` (1..32) copies in flight per
- *    warp, 4 warps per block; 4 * depth * unit_bytes <= 200 KB.
+ *  GMR_GATHER_BULK: one bulk copy (cp.async.bulk) per random unit into shared
+ *    memory, `depth` (even, 2..64) copies in flight per warp in two stages of
+ *    depth/2 copies that complete on one mbarrier phase each, 4 warps per
+ *    block; 4 * depth * unit_bytes <= 200 KB.
  * unit_bytes: a power of two in [16, 16384] (at least one lane access).
  * gmr_measure_gather_bandwidth is GMR_GATHER_LOAD16 (or SEQ16), depth 4,
  * 128-byte units.  GMR_ERR_TIMEOUT if a bulk-copy wait gave up. */

@@ -28,8 +28,8 @@ def test_gather_load_paths(mode, depth, unit):
     assert 100.0 < gbs < 50000.0
 
 
-@pytest.mark.parametrize("kw", [dict(mode="bulk", depth=33), dict(mode="load16", depth=3),
-                                dict(mode="load32", unit_bytes=16), dict(mode="bulk", depth=32, unit_bytes=4096),
+@pytest.mark.parametrize("kw", [dict(mode="bulk", depth=66), dict(mode="bulk", depth=3), dict(mode="load16", depth=3),
+                                dict(mode="load32", unit_bytes=16), dict(mode="bulk", depth=64, unit_bytes=4096),
                                 dict(unit_bytes=96)])
 def test_gather_rejects_bad_arguments(kw):
     """Checked on the host before any device work."""

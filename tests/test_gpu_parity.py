@@ -104,6 +104,13 @@ CONFIGS = [
     dict(variant=gmr.VARIANT_GRAPH, push=gmr.PUSH_ALWAYS),                 # rules push their emissions
     dict(variant=gmr.VARIANT_FUSED, push=gmr.PUSH_ALWAYS, emit_mode=gmr.EMIT_ROWS, vec_tile=4, tile_levels=2),
     dict(variant=gmr.VARIANT_FUSED, push=gmr.PUSH_ALWAYS, emit_mode=gmr.EMIT_ATOMIC),
+    # 32-byte lane accesses (8 words per lane) where the tile allows them
+    dict(variant=gmr.VARIANT_GRAPH, lane_bytes=32),
+    dict(variant=gmr.VARIANT_PERSISTENT, lane_bytes=32),
+    dict(variant=gmr.VARIANT_FUSED, lane_bytes=32, emit_mode=gmr.EMIT_ROWS, vec_tile=8, tile_levels=2),
+    dict(variant=gmr.VARIANT_FUSED, lane_bytes=32, emit_mode=gmr.EMIT_ATOMIC, vec_tile=16),
+    dict(variant=gmr.VARIANT_GRAPH, lane_bytes=32, push=gmr.PUSH_ALWAYS, emit_mode=gmr.EMIT_SEGMENTED,
+         ops_per_cta=5),
 ]
 
 
@@ -117,6 +124,26 @@ def test_golden_batched(case, sr, B):
     for cfg in CONFIGS:
         Y = engine_outputs(sr, eng.multiply(engine_inputs(sr, X), sr, B=B, **cfg), B)
         check(sr, Y, ref)
+
+
+@pytest.mark.parametrize("sr", [0, 2])
+@pytest.mark.parametrize("B", [8, 32, 128])
+def test_wide_lanes_every_level_table(case, sr, B, monkeypatch):
+    """32-byte lane accesses as the engine default (GMR_LANE_BYTES=32):
+    every per-launch table (folds, grids, source chunks, push, interleave)
+    matches the oracle."""
+    monkeypatch.setenv("GMR_LANE_BYTES", "32")
+    monkeypatch.setenv("GMR_CHUNK_SLOTS", "5")
+    rows, cols = int(case["rows"]), int(case["cols"])
+    X = random_X(sr, cols, B, 700 + B)
+    ref = oracle_columns(case["sched"], sr, case["V"], X, rows, cols)
+    eng = gmr.Engine(case["plan"])
+    Xw = engine_inputs(sr, X)
+    for table in ([v] * (eng.depth + 2) for v in (0, 3, 4, 10, 13, 32, 35, 45, 64, 67, 77)):
+        eng.set_level_variants(sr, B, table)
+        check(sr, eng.multiply(Xw, sr, B=B), ref)
+    eng.set_level_variants(sr, B, None)
+    check(sr, eng.multiply(Xw, sr, B=B, variant=gmr.VARIANT_PERSISTENT), ref)
 
 
 @pytest.mark.parametrize("sr", range(3))
