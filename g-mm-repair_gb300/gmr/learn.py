@@ -189,7 +189,7 @@ def random_inputs(torch, semiring: int, cols: int, B: int, seed: int):
 
 
 def record(eng: Engine, plan: Plan, semiring: int, B: int, seed: int, reps: int = 3):
-    """Autotuner timings of every (launch, variant) -> (inputs [slots*V][26], log us [slots*V], times [slots][V])."""
+    """Autotuner timings of every (launch, variant) -> (inputs, log us, times [slots][V] ms, base features)."""
     import torch
 
     X, words = random_inputs(torch, semiring, eng.cols, B, seed)
@@ -197,10 +197,15 @@ def record(eng: Engine, plan: Plan, semiring: int, B: int, seed: int, reps: int 
     stream = torch.cuda.current_stream().cuda_stream
     times = eng.autotune(semiring, X.data_ptr(), Y.data_ptr(), B, stream=stream, reps=reps)
     base = launch_features(plan, semiring, B)
+    return training_rows(base, times) + (times, base)
+
+
+def training_rows(base: np.ndarray, times: np.ndarray):
+    """Model inputs and targets (log us) of every (launch, variant) but the prologue slot's."""
     Xin = model_inputs(base)
     T = np.log(np.maximum(times.reshape(-1), 1e-4) * 1000.0).astype(np.float32)  # ms -> log us
     keep = np.repeat(np.arange(base.shape[0]) >= 1, N_VAR)  # drop the prologue slot
-    return Xin[keep], T[keep], times
+    return Xin[keep], T[keep]
 
 
 def sweep_time(eng: Engine, semiring: int, B: int, table, seed: int, n: int = 10) -> float:
@@ -248,6 +253,9 @@ def main():
     ap.add_argument("--Bs", default="1,8,32,128")
     ap.add_argument("--epochs", type=int, default=80)
     ap.add_argument("--small", action="store_true", help="the earlier small size ranges")
+    ap.add_argument("--resume", default=None,
+                    help="a directory holding rec_<grammar>.npz files of an earlier run: those grammars are loaded, "
+                         "not recorded again")
     args = ap.parse_args()
     out = Path(args.out)
     out.mkdir(parents=True, exist_ok=True)
@@ -260,22 +268,37 @@ def main():
     rows_tr, rows_te = [], []
     t0 = time.time()
     for gi, spec in enumerate(specs):
-        g, rows, cols = make_grammar(spec, device=0)
-        plan = Plan.build(g, rows, cols, device=0)
-        eng = Engine(plan)
-        for sr in (0, 1, 2):
-            for B in Bs:
-                seed = 1000 * gi + 10 * sr + B
-                Xin, T, times = record(eng, plan, sr, B, seed)
-                rec = dict(g=gi, sr=sr, B=B, X=Xin, T=T, times=times, ops=plan.stats["n_ops"])
-                (rows_te if gi in hold else rows_tr).append(rec)
-        print(json.dumps(dict(grammar=gi, spec=spec, ops=plan.stats["n_ops"], depth=plan.stats["depth"],
-                              held_out=gi in hold, elapsed_s=round(time.time() - t0, 1))), flush=True)
-        del eng
+        # each grammar's records are saved as they are made (rec_<gi>.npz), so
+        # that a run cut short can be resumed from its output directory
+        done = [Path(d) / f"rec_{gi}.npz" for d in (args.resume, out) if d]
+        done = [f for f in done if f.exists()]
+        if done:
+            z = np.load(done[0], allow_pickle=False)
+            recs = []
+            for i in range(len(z["sr"])):
+                Xin, T = training_rows(z[f"base{i}"], z[f"times{i}"])
+                recs.append(dict(g=gi, sr=int(z["sr"][i]), B=int(z["B"][i]), X=Xin, T=T, times=z[f"times{i}"]))
+            info = dict(grammar=gi, loaded=str(done[0]))
+        else:
+            g, rows, cols = make_grammar(spec, device=0)
+            plan = Plan.build(g, rows, cols, device=0)
+            eng = Engine(plan)
+            recs = []
+            for sr in (0, 1, 2):
+                for B in Bs:
+                    seed = 1000 * gi + 10 * sr + B
+                    Xin, T, times, base = record(eng, plan, sr, B, seed)
+                    recs.append(dict(g=gi, sr=sr, B=B, X=Xin, T=T, times=times, base=base))
+            arrays = {"sr": np.array([r["sr"] for r in recs]), "B": np.array([r["B"] for r in recs])}
+            for i, r in enumerate(recs):
+                arrays.update({f"base{i}": r["base"], f"times{i}": r["times"]})
+            np.savez_compressed(out / f"rec_{gi}.npz", **arrays)
+            info = dict(grammar=gi, spec=spec, ops=plan.stats["n_ops"], depth=plan.stats["depth"])
+            del eng
+        (rows_te if gi in hold else rows_tr).extend(recs)
+        print(json.dumps(info | dict(held_out=gi in hold, elapsed_s=round(time.time() - t0, 1))), flush=True)
     Xtr = np.concatenate([r["X"] for r in rows_tr])
     Ttr = np.concatenate([r["T"] for r in rows_tr])
-    np.savez_compressed(out / "dataset.npz", Xtr=Xtr, Ttr=Ttr, Xte=np.concatenate([r["X"] for r in rows_te]),
-                        Tte=np.concatenate([r["T"] for r in rows_te]))
     model = Mlp.create(seed=1)
     mean, std = Xtr.mean(axis=0), Xtr.std(axis=0)
     std[std < 1e-6] = 1.0
