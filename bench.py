@@ -881,7 +881,11 @@ def main():
                 learned_ms = timed(30)
                 tuning["learned_vps"] = B * 1000.0 / learned_ms
                 tuning["learned_regret_vs_autotuner"] = learned_ms / auto_ms - 1.0
-                tuning["headline"] = "learned"
+                if learned_ms <= 1.10 * auto_ms:
+                    tuning["headline"] = "learned"
+                else:  # the learned pick falls back to the autotuner's measured choice
+                    eng.set_level_variants(sr, B, tuning["autotuned_table"])
+                    tuning["headline"] = "autotuned (the learned pick was more than 10 % slower)"
             else:
                 tuning["headline"] = "autotuned (no trained cost model present)"
 

@@ -247,6 +247,11 @@ struct LevelArgs {
     // launch then folds nothing of this level.  nullptr: pulled as usual.
     const int32_t* pe_off = nullptr;
     const int32_t* pe_row = nullptr;
+    // Staging (k_level_staged): bytes of the shared-memory window, and the
+    // error word a wait that gives up sets (err[0] = 1, err[1] = -(level)).
+    int stage_bytes = 0;
+    int* err = nullptr;
+    int level = 0;
 };
 
 template <int GLOG>
@@ -604,6 +609,125 @@ __global__ void __launch_bounds__(256, VEC == 8 ? 4 : 1) k_level(SweepArgs a, Le
     }
 }
 
+// Shared-memory staging of the left-child window (GMR_LEVEL_STAGE).  Rules of
+// a level are sorted by left child, so the slot children of R consecutive
+// rules lie in one window [lo, hi] of the arena.  An ops block takes runs of
+// R = 2 * (256 / G) rules; for each run one thread posts the window's byte
+// count on an mbarrier and issues ONE bulk copy (cp.async.bulk) of the window
+// into shared memory when it fits in L.stage_bytes, while every thread loads
+// its rules and right children from global memory; the left children are
+// then read from shared memory.  Runs whose window does not fit (or holds no
+// slot) read both children from global memory.  Emission blocks fold as
+// k_level's segmented fold.  The wait is bounded: after the limit the block
+// sets L.err, waits (again bounded) for its copy and returns.
+static constexpr int kStageBytes = 47 * 1024;  // with the static words, within the 48 KB a block gets without opting in
+static constexpr unsigned long long kStageSpinLimit = 20000000ull;
+
+template <class S, int VEC, int GLOG>
+__global__ void __launch_bounds__(256, VEC == 8 ? 4 : 1) k_level_staged(SweepArgs a, LevelArgs L) {
+    static_assert(GLOG >= 0 && VEC >= 4, "staging needs a power-of-two lane count and 16-byte values");
+    using T = typename S::T;
+    extern __shared__ __align__(128) unsigned char win_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ long long s_lo, s_hi;
+    __shared__ int s_use, s_ok;
+    const int tile = a.t0 + blockIdx.y;
+    if ((int)blockIdx.x < L.em_blocks) {
+        emits_t<S, VEC, GLOG, GMR_EMIT_SEGMENTED, false, false>(
+            a, L, tile, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, (int64_t)L.em_blocks * blockDim.x);
+        return;
+    }
+    constexpr int kUnits = 256 >> GLOG;  // rules per pass of the block
+    constexpr int R = 2 * kUnits;        // rules per run
+    const Values<S, VEC> val(a, tile);
+    const T* arena_t = static_cast<const T*>(a.arena) + (int64_t)tile * a.n_ops * a.Bt;
+    T* out = static_cast<T*>(a.arena) + (int64_t)tile * a.n_ops * a.Bt;
+    const T* win = reinterpret_cast<const T*>(win_raw);
+    const int u = threadIdx.x >> GLOG, lane = threadIdx.x & ((1 << GLOG) - 1);
+    const int ob = (int)blockIdx.x - L.em_blocks, nob = (int)gridDim.x - L.em_blocks;
+    const int2* ops = L.ops + L.op_first;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    for (int64_t r0 = (int64_t)ob * R; r0 < L.n_ops; r0 += (int64_t)nob * R) {
+        const int64_t r1 = min(r0 + (int64_t)R, L.n_ops);
+        if (threadIdx.x == 0) {
+            int64_t lo_i = r0, hi_i = r1;  // first rule whose left child is a slot
+            while (lo_i < hi_i) {
+                const int64_t mid = (lo_i + hi_i) >> 1;
+                if (__ldg(&ops[mid].x) >= 0) hi_i = mid;
+                else lo_i = mid + 1;
+            }
+            int use = 0;
+            long long lo = 0, hi = -1;
+            if (lo_i < r1) {
+                lo = __ldg(&ops[lo_i].x);
+                hi = __ldg(&ops[r1 - 1].x);
+                const long long bytes = (hi - lo + 1) * (long long)a.Bt * 4;
+                if (bytes <= L.stage_bytes) {
+                    use = 1;
+                    fence_proxy_async_smem();  // the previous run's reads of the window come first
+                    mbar_arrive_expect_tx(&bar, (uint32_t)bytes);
+                    bulk_g2s(win_raw, arena_t + lo * a.Bt, (uint32_t)bytes, &bar);
+                }
+            }
+            s_use = use;
+            s_lo = lo;
+            s_hi = hi;
+        }
+        __syncthreads();
+        const int use = s_use;
+        const long long lo = s_lo, hi = s_hi;
+        const int64_t ia = r0 + u, ib = r0 + u + kUnits;
+        const bool ha = ia < r1, hb = ib < r1;
+        const int2 oa = ha ? __ldg(ops + ia) : make_int2(-1, -1);
+        const int2 ob2 = hb ? __ldg(ops + ib) : make_int2(-1, -1);
+        Vec<T, VEC> ra_v = val.get(oa.y, lane), rb_v = val.get(ob2.y, lane);
+        Vec<T, VEC> la_v, lb_v;
+        if (use) {
+            if (threadIdx.x == 0) s_ok = mbar_wait(&bar, phase, kStageSpinLimit) ? 1 : 0;
+            __syncthreads();
+            if (!s_ok) {
+                if (threadIdx.x == 0) {
+                    L.err[1] = -L.level;
+                    __threadfence();
+                    atomicExch(L.err, 1);
+                    mbar_wait(&bar, phase, kStageSpinLimit);  // the copy still lands in this block's memory
+                }
+                __syncthreads();
+                return;
+            }
+            phase ^= 1u;
+            // a child outside [lo, hi] (not possible for a level sorted by
+            // left child, checked anyway) is read from global memory
+            la_v = oa.x >= lo && oa.x <= hi
+                       ? *reinterpret_cast<const Vec<T, VEC>*>(win + (oa.x - lo) * a.Bt + lane * VEC)
+                       : val.get(oa.x, lane);
+            lb_v = ob2.x >= lo && ob2.x <= hi
+                       ? *reinterpret_cast<const Vec<T, VEC>*>(win + (ob2.x - lo) * a.Bt + lane * VEC)
+                       : val.get(ob2.x, lane);
+        } else {
+            la_v = val.get(oa.x, lane);
+            lb_v = val.get(ob2.x, lane);
+        }
+        if (L.op_c) {
+            const float ca = ha ? __ldg(L.op_c + L.op_first + ia) : 1.0f;
+            const float cb = hb ? __ldg(L.op_c + L.op_first + ib) : 1.0f;
+#pragma unroll
+            for (int j = 0; j < VEC; ++j) {
+                la_v.v[j] = S::apply(la_v.v[j], ca);
+                lb_v.v[j] = S::apply(lb_v.v[j], cb);
+            }
+        }
+        if (ha) vstore<T, VEC>(out + (L.op_first + ia) * a.Bt + lane * VEC, voplus<S, VEC>(la_v, ra_v));
+        if (hb) vstore<T, VEC>(out + (L.op_first + ib) * a.Bt + lane * VEC, voplus<S, VEC>(lb_v, rb_v));
+        __syncthreads();  // every read of the window is done before the next run's copy
+    }
+}
+
 // Persistent sweep: one cooperative launch walks the prologue and every
 // level, separated by grid barriers.  Each barrier wait is bounded: a block
 // that waits longer than spin_limit polls (or sees another block's failure)
@@ -877,8 +1001,9 @@ struct gmr_engine {
     std::vector<int64_t> le_off;
     int64_t n_left_split = 0;
     bool left_ready = false;
-    int* status_host = nullptr;                           // pinned copy of the last persistent error words
-    bool last_persistent = false;
+    int* status_host = nullptr;                           // pinned copy of the last error words
+    bool last_persistent = false;  // the last multiply reported error words (persistent or staged launches)
+    int* stage_err() { return reinterpret_cast<int*>(static_cast<unsigned char*>(sync.p) + 8); }
     cudaStream_t own_stream = nullptr;
     std::vector<gmr::GraphEntry> graphs;
     std::map<std::pair<int, int>, std::vector<uint8_t>> level_variants;  // (semiring, B) -> per-launch variant
@@ -930,6 +1055,23 @@ static int level_mode(const gmr_engine* e, const Launch& lc, int k) {
     if ((lc.lv[k] & GMR_LEVEL_INTERLEAVE) && can_interleave(e, lc, k)) return kFoldInterleave;
     if ((lc.lv[k] & GMR_LEVEL_PUSH) && can_push(e, k)) return kFoldPush;
     return kFoldPull;
+}
+
+// Whether the rules of level k run k_level_staged (GMR_LEVEL_STAGE in the
+// installed table): per-level chains only, plain references (no direct
+// terminal codes), 16- or 32-byte lanes in power-of-two groups, and a level
+// that does not push its emissions.
+static bool level_staged(const gmr_engine* e, const Launch& lc, int k) {
+    if (lc.variant == GMR_VARIANT_PLAIN || lc.variant == GMR_VARIANT_PERSISTENT) return false;
+    if (lc.lv.empty() || k < 1 || k > e->depth || k >= (int)lc.lv.size() || !(lc.lv[k] & GMR_LEVEL_STAGE)) return false;
+    if (e->direct_terms || lc.VEC < 4 || (lc.G & (lc.G - 1)) != 0 || lc.G > 32) return false;
+    return level_mode(e, lc, k) != kFoldPush;
+}
+
+static bool any_staged(const gmr_engine* e, const Launch& lc) {
+    for (int k = 1; k <= e->depth; ++k)
+        if (level_staged(e, lc, k)) return true;
+    return false;
 }
 
 // Optional per-launch timing: an event is recorded before the first launch
@@ -1026,7 +1168,7 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
         int emit = lc.emit, chunk = lc.chunk, ops_cap = kOpsCtasPerSm[0];
         bool by_chunk = false;
         if (!lc.lv.empty() && slot < (int)lc.lv.size()) {
-            const int v = (lc.lv[slot] & ~(GMR_LEVEL_PUSH | GMR_LEVEL_INTERLEAVE)) % GMR_N_LEVEL_VARIANTS;
+            const int v = (lc.lv[slot] & ~(GMR_LEVEL_PUSH | GMR_LEVEL_INTERLEAVE | GMR_LEVEL_STAGE)) % GMR_N_LEVEL_VARIANTS;
             emit = kEmitVariants[v % kNumEmitVariants].emit;
             chunk = kEmitVariants[v % kNumEmitVariants].chunk;
             ops_cap = kOpsCtasPerSm[(v / kNumEmitVariants) % 2];
@@ -1075,6 +1217,10 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
             L.seg_first = e->seg_off[k_em];
             nseg = e->seg_off[k_em + 1] - e->seg_off[k_em];
         }
+        auto em_items_seg = [&](int64_t ne) -> int64_t {  // the segmented fold, chunk 16
+            if (GLOG == 0) return (ne + 1) / 2;
+            return (ne + 15) / 16 * lc.G;
+        };
         auto em_items = [&](int64_t ne, int64_t ns) -> int64_t {
             if (emit == GMR_EMIT_ATOMIC) return ne * lc.G;
             if (emit == GMR_EMIT_ROWS) return ns * lc.G;
@@ -1091,12 +1237,28 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
                 if (t_timer && mark && !split) t_timer->mark();  // keep one timing slot per level launch
                 return;
             }
+            const int dirk = !M.direct_ops ? 0 : M.direct ? 2 : 1;
+            if constexpr (GLOG >= 0 && VEC >= 4) {
+                if (no > 0 && dirk == 0 && k_ops >= 1 && level_staged(e, lc, k_ops)) {
+                    // staged rules; the launch's emissions use the segmented fold
+                    const int64_t R = 2 * (256 >> GLOG);
+                    const int eb = ne > 0 ? blocks_for(em_items_seg(ne), nt) : 0;
+                    const int ob = (int)std::min<int64_t>((no + R - 1) / R, std::max(1, e->sm_count * ops_cap / nt));
+                    M.em_blocks = eb;
+                    M.em_chunk = 16;
+                    M.stage_bytes = kStageBytes;
+                    M.err = e->stage_err();
+                    M.level = k_ops;
+                    k_level_staged<S, VEC, GLOG><<<dim3(eb + ob, nt), 256, kStageBytes, st>>>(s, M);
+                    after(mark);
+                    return;
+                }
+            }
             int eb = ne > 0 ? blocks_for(em_items(ne, ns), nt) : 0;
             int ob = no > 0 ? std::min<int>(blocks_for((no * lc.G + 1) / 2, nt),
                                             std::max(1, e->sm_count * ops_cap / nt)) : 0;
             M.em_blocks = eb;
             dim3 grid(eb + ob, nt);
-            const int dirk = !M.direct_ops ? 0 : M.direct ? 2 : 1;
             if (dirk == 0) launch_level<S, VEC, GLOG, 0>(emit, grid, st, s, M);
             else if (dirk == 1) launch_level<S, VEC, GLOG, 1>(emit, grid, st, s, M);
             else launch_level<S, VEC, GLOG, 2>(emit, grid, st, s, M);
@@ -1126,6 +1288,8 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
         }
     };
     const int D = e->depth;
+    const bool staged = any_staged(e, lc);
+    if (staged) GMR_CUDA(cudaMemsetAsync(e->stage_err(), 0, 8, st));  // the staged waits' error words
     if (lc.variant == GMR_VARIANT_PLAIN) {
         level(0, 0, 0, lc.ntile, true);  // terminal emissions
         for (int k = 1; k <= D; ++k) {
@@ -1153,6 +1317,7 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
         }
         level(0, D, 0, lc.ntile, false);
     }
+    if (staged) GMR_CUDA(cudaMemcpyAsync(e->status_host, e->stage_err(), 8, cudaMemcpyDeviceToHost, st));
     GMR_CUDA(cudaGetLastError());
 }
 
@@ -1417,6 +1582,7 @@ static void multiply_device(gmr_engine* e, int semiring, const void* X, void* Y,
     } else {
         launch_chain(e, lc, X, Y, st, launches);
     }
+    if (any_staged(e, lc)) e->last_persistent = true;
     e->last_launches = launches;
 }
 
@@ -1656,7 +1822,7 @@ extern "C" int gmr_engine_multiply_host(gmr_engine* e, int semiring, const void*
         if (yb) GMR_CUDA(cudaMemcpyAsync(hY, e->hY.p, yb, cudaMemcpyDeviceToHost, st));
         GMR_CUDA(cudaStreamSynchronize(st));
         if (e->last_persistent && e->status_host[0] != 0)
-            throw Error(GMR_ERR_TIMEOUT, "persistent sweep: a grid-barrier wait gave up at phase " +
+            throw Error(GMR_ERR_TIMEOUT, "a bounded device-side wait gave up at phase " +
                                              std::to_string(e->status_host[1]) + "; Y is not valid");
     });
 }
@@ -1703,7 +1869,7 @@ extern "C" int gmr_engine_multiply_host_many(gmr_engine* e, int semiring, const 
         GMR_CUDA(cudaStreamSynchronize(e->copy_out));
         GMR_CUDA(cudaStreamSynchronize(st));
         if (e->last_persistent && e->status_host[0] != 0)
-            throw Error(GMR_ERR_TIMEOUT, "persistent sweep: a grid-barrier wait gave up at phase " +
+            throw Error(GMR_ERR_TIMEOUT, "a bounded device-side wait gave up at phase " +
                                              std::to_string(e->status_host[1]) + "; Y is not valid");
     });
 }
@@ -1743,7 +1909,7 @@ extern "C" int gmr_engine_set_level_variants(gmr_engine* e, int semiring, int B,
         }
         if (n != e->depth + 2) throw Error(GMR_ERR_ARG, "need depth + 2 = " + std::to_string(e->depth + 2) + " entries");
         for (int i = 0; i < n; ++i) {
-            if ((v[i] & ~(GMR_LEVEL_PUSH | GMR_LEVEL_INTERLEAVE)) >= GMR_N_LEVEL_VARIANTS)
+            if ((v[i] & ~(GMR_LEVEL_PUSH | GMR_LEVEL_INTERLEAVE | GMR_LEVEL_STAGE)) >= GMR_N_LEVEL_VARIANTS)
                 throw Error(GMR_ERR_ARG, "variant index out of range");
             if ((v[i] & GMR_LEVEL_PUSH) && (v[i] & GMR_LEVEL_INTERLEAVE))
                 throw Error(GMR_ERR_ARG, "a level cannot both push and interleave");
@@ -1838,28 +2004,28 @@ extern "C" int gmr_engine_autotune_energy(gmr_engine* e, int semiring, const voi
         };
         bool any_mode = false;
         for (int k = 1; k <= D; ++k) any_mode |= allowed(k, kFoldPush) || allowed(k, kFoldInterleave);
+        auto slot_times = [&](const std::vector<uint8_t>& table) {
+            if (gmr_engine_set_level_variants(e, semiring, B, table.data(), nl) != GMR_OK)
+                throw Error(GMR_ERR_ARG, gmr_last_error());
+            std::vector<std::vector<float>> runs;
+            for (int r = 0; r < reps; ++r) {
+                int n = 0;
+                gmr_config c{};
+                int rc = gmr_engine_time_launches(e, semiring, dX, dY, B, &c, stream, buf.data(), (int)buf.size(), &n);
+                if (rc != GMR_OK) throw Error(rc, gmr_last_error());
+                if (n != nl) throw Error(GMR_ERR_STATE, "unexpected launch count " + std::to_string(n));
+                runs.emplace_back(buf.begin(), buf.begin() + n);
+            }
+            std::vector<float> out(nl);
+            for (int l = 0; l < nl; ++l) {
+                std::vector<float> xs;
+                for (auto& r : runs) xs.push_back(r[l]);
+                std::nth_element(xs.begin(), xs.begin() + xs.size() / 2, xs.end());
+                out[l] = xs[xs.size() / 2];
+            }
+            return out;
+        };
         if (any_mode) {
-            auto slot_times = [&](const std::vector<uint8_t>& table) {
-                if (gmr_engine_set_level_variants(e, semiring, B, table.data(), nl) != GMR_OK)
-                    throw Error(GMR_ERR_ARG, gmr_last_error());
-                std::vector<std::vector<float>> runs;
-                for (int r = 0; r < reps; ++r) {
-                    int n = 0;
-                    gmr_config c{};
-                    int rc = gmr_engine_time_launches(e, semiring, dX, dY, B, &c, stream, buf.data(), (int)buf.size(), &n);
-                    if (rc != GMR_OK) throw Error(rc, gmr_last_error());
-                    if (n != nl) throw Error(GMR_ERR_STATE, "unexpected launch count " + std::to_string(n));
-                    runs.emplace_back(buf.begin(), buf.begin() + n);
-                }
-                std::vector<float> out(nl);
-                for (int l = 0; l < nl; ++l) {
-                    std::vector<float> xs;
-                    for (auto& r : runs) xs.push_back(r[l]);
-                    std::nth_element(xs.begin(), xs.begin() + xs.size() / 2, xs.end());
-                    out[l] = xs[xs.size() / 2];
-                }
-                return out;
-            };
             const uint8_t flag[3] = {0, GMR_LEVEL_PUSH, GMR_LEVEL_INTERLEAVE};
             const float kUnset = -1.0f;
             // cost[k][3 * m_prev + m]: slot k with level k-1 in m_prev and level k in m
@@ -1905,6 +2071,17 @@ extern "C" int gmr_engine_autotune_energy(gmr_engine* e, int semiring, const voi
                     m = from[k][m];
                 }
             }
+        }
+        // Shared-memory staging of the left-child window: it changes only the
+        // launch of its own level, so each level keeps it where that launch
+        // measured at least 2 % faster with it.
+        if (D >= 1) {
+            std::vector<uint8_t> st_table = best;
+            for (int k = 1; k <= D; ++k)
+                if (!(best[k] & GMR_LEVEL_PUSH)) st_table[k] |= GMR_LEVEL_STAGE;
+            const std::vector<float> base_t = slot_times(best), st_t = slot_times(st_table);
+            for (int k = 1; k <= D; ++k)
+                if (st_table[k] != best[k] && st_t[k] < 0.98f * base_t[k]) best[k] = st_table[k];
         }
         if (gmr_engine_set_level_variants(e, semiring, B, best.data(), nl) != GMR_OK) throw Error(GMR_ERR_ARG, gmr_last_error());
         if (ms) std::copy(med.begin(), med.end(), ms);

@@ -22,6 +22,7 @@
 // The reference's own layered figures (L, w*, |R|, +pt, E, E_T, U) are
 // computed alongside for reporting and for the roofline byte count.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -648,6 +649,58 @@ extern "C" double gmr_plan_alg_bytes(const gmr_plan* p, int semiring, int B) {
            4.0 * (double)s.rows * Bp;
 }
 
+// Left-child windows of shared-memory staging: within a level the rules are
+// sorted by left child, so the arena slots that the left children of a run of
+// consecutive rules (one CTA's rules) reference form one contiguous window
+// [first slot child, last child].  Per level k (row k-1 of out): fractions of
+// the level's runs of rules_per_cta rules whose window holds at most 64 KB,
+// 128 KB and 200 KB of values of `words` 4-byte words; the mean density of
+// the windows (distinct referenced slots / window slots); and the fraction of
+// left children that are slots (the rest are terminals).
+static void window_stats(const gmr_plan& p, int rules_per_cta, int words, double* out) {
+    const double budget[3] = {64.0 * 1024, 128.0 * 1024, 200.0 * 1024};
+    for (int k = 1; k <= p.depth; ++k) {
+        double* o = out + (size_t)(k - 1) * GMR_WINDOW_STATS;
+        std::fill(o, o + GMR_WINDOW_STATS, 0.0);
+        const int64_t a = p.lvl_off[k - 1], b = p.lvl_off[k];
+        int64_t runs = 0, slot_refs = 0, dens_runs = 0;
+        double dens = 0.0;
+        for (int64_t r0 = a; r0 < b; r0 += rules_per_cta) {
+            const int64_t r1 = std::min<int64_t>(r0 + rules_per_cta, b);
+            ++runs;
+            int64_t lo = -1, hi = -1, distinct = 0;
+            int32_t prev = INT32_MIN;
+            for (int64_t i = r0; i < r1; ++i) {
+                const int32_t c = p.op_l[(size_t)i];
+                if (c < 0) continue;
+                ++slot_refs;
+                if (lo < 0) lo = c;
+                hi = c;
+                distinct += c != prev;
+                prev = c;
+            }
+            const double bytes = lo < 0 ? 0.0 : (double)(hi - lo + 1) * words * 4.0;
+            for (int j = 0; j < 3; ++j) o[j] += bytes <= budget[j];
+            if (lo >= 0) {
+                dens += (double)distinct / (double)(hi - lo + 1);
+                ++dens_runs;
+            }
+        }
+        if (runs) for (int j = 0; j < 3; ++j) o[j] /= (double)runs;
+        o[3] = dens_runs ? dens / (double)dens_runs : 0.0;
+        o[4] = b > a ? (double)slot_refs / (double)(b - a) : 0.0;
+    }
+}
+
+extern "C" int gmr_plan_window_stats(const gmr_plan* p, int rules_per_cta, int words, double* out, int cap, int* n) {
+    return guarded([&] {
+        if (!p || !out || !n || rules_per_cta < 1 || words < 1) throw Error(GMR_ERR_ARG, "bad argument");
+        if (cap < p->depth * GMR_WINDOW_STATS) throw Error(GMR_ERR_RANGE, "need depth x GMR_WINDOW_STATS doubles");
+        window_stats(*p, rules_per_cta, words, out);
+        *n = p->depth;
+    });
+}
+
 extern "C" int gmr_plan_describe(const gmr_plan* p, char* buf, size_t cap) {
     return guarded([&] {
         if (!p || !buf || cap == 0) throw Error(GMR_ERR_ARG, "bad argument");
@@ -669,6 +722,15 @@ extern "C" int gmr_plan_describe(const gmr_plan* p, char* buf, size_t cap) {
         for (int k = 1; k <= p->depth; ++k) {
             std::snprintf(line, sizeof line, "%d\t%lld\t%lld\n", k, (long long)(p->lvl_off[k] - p->lvl_off[k - 1]),
                           (long long)(p->em_off[k + 1] - p->em_off[k]));
+            o += line;
+        }
+        std::vector<double> ws((size_t)std::max(p->depth, 1) * GMR_WINDOW_STATS);
+        window_stats(*p, 128, 32, ws.data());
+        o += "Left-child windows of 128 rules at 32 words per value: level, share fitting 64/128/200 KB, "
+             "density, slot share\n";
+        for (int k = 1; k <= p->depth; ++k) {
+            const double* w = ws.data() + (size_t)(k - 1) * GMR_WINDOW_STATS;
+            std::snprintf(line, sizeof line, "%d\t%.2f\t%.2f\t%.2f\t%.2f\t%.2f\n", k, w[0], w[1], w[2], w[3], w[4]);
             o += line;
         }
         std::snprintf(buf, cap, "%s", o.c_str());

@@ -31,7 +31,7 @@ TROPICAL_INF = 1_000_000_000
 VARIANT_AUTO, VARIANT_PLAIN, VARIANT_FUSED, VARIANT_GRAPH, VARIANT_PERSISTENT = 0, 1, 2, 3, 4
 EMIT_AUTO, EMIT_ATOMIC, EMIT_SEGMENTED, EMIT_ROWS = 0, 1, 2, 3
 PUSH_AUTO, PUSH_NEVER, PUSH_ALWAYS, PUSH_INTERLEAVE = 0, 1, 2, 3
-LEVEL_PUSH, LEVEL_INTERLEAVE = 32, 64
+LEVEL_PUSH, LEVEL_INTERLEAVE, LEVEL_STAGE = 32, 64, 128
 
 __all__ = [
     "GmrError", "Csrv", "Grammar", "Plan", "Engine", "gen_mosaic", "gen_copy_graph", "repair", "semiring_id",
@@ -341,6 +341,17 @@ class Plan:
     def prepare_left(self):
         """Builds the reverse adjacency for the left product (y = x^T M)."""
         _check(lib().gmr_plan_prepare_left(self._h))
+
+    def window_stats(self, rules_per_cta: int = 128, words: int = 32) -> np.ndarray:
+        """[depth][5] per level: share of runs of rules_per_cta rules whose
+        left-child window fits 64 / 128 / 200 KB of `words`-word values, mean
+        window density, share of left children that are slots."""
+        d = max(self.stats["depth"], 1)
+        out = np.zeros(d * 5, dtype=np.float64)
+        n = C.c_int()
+        _check(lib().gmr_plan_window_stats(self._h, int(rules_per_cta), int(words),
+                                           out.ctypes.data_as(L.F64P), len(out), C.byref(n)))
+        return out[: n.value * 5].reshape(n.value, 5)
 
     def describe(self) -> str:
         cap = 1 << 16

@@ -106,6 +106,7 @@ _SIGS = {
     "gmr_plan_alg_bytes": (C.c_double, [P, C.c_int, C.c_int]),
     "gmr_plan_array": (C.c_int, [P, C.c_int, C.POINTER(P), C.POINTER(C.c_int64)]),
     "gmr_plan_describe": (C.c_int, [P, C.c_char_p, C.c_size_t]),
+    "gmr_plan_window_stats": (C.c_int, [P, C.c_int, C.c_int, F64P, C.c_int, C.POINTER(C.c_int)]),
     "gmr_plan_free": (None, [P]),
     "gmr_engine_create": (C.c_int, [P, C.c_int, C.POINTER(P)]),
     "gmr_engine_multiply": (C.c_int, [P, C.c_int, P, P, C.c_int, C.POINTER(Config), P]),

@@ -219,8 +219,20 @@ double gmr_plan_alg_bytes(const gmr_plan* p, int semiring, int B);
  * 21 le_tgt (int32), 22 le_split (int32) (see gmr_plan_prepare_left).
  * *ptr stays valid until gmr_plan_free. */
 int gmr_plan_array(const gmr_plan* p, int which, const void** ptr, int64_t* n);
-/* Human-readable per-level report (the host_scheduler inspector). */
+/* Human-readable per-level report (the host_scheduler inspector), with the
+ * left-child window statistics below at 128 rules per CTA and 32 words. */
 int gmr_plan_describe(const gmr_plan* p, char* buf, size_t cap);
+/* Left-child windows for shared-memory staging.  Within a level the rules
+ * are sorted by left child, so the arena slots referenced by the left
+ * children of rules_per_cta consecutive rules form one window [first, last].
+ * For each level k = 1..depth, out[(k-1) * GMR_WINDOW_STATS + j]: j = 0, 1, 2
+ * the share of the level's runs of rules_per_cta rules whose window holds at
+ * most 64 / 128 / 200 KB of values of `words` 4-byte words; j = 3 the mean
+ * density of the windows (distinct referenced slots / window slots); j = 4
+ * the share of left children that are slots (the others are terminals).
+ * *n = depth. */
+#define GMR_WINDOW_STATS 5
+int gmr_plan_window_stats(const gmr_plan* p, int rules_per_cta, int words, double* out, int cap, int* n);
 void gmr_plan_free(gmr_plan* p);
 
 /* ------------------------------------------------------------------ */
@@ -315,6 +327,18 @@ int gmr_engine_time_launches(gmr_engine* e, int semiring, const void* dX, void* 
 #define GMR_N_LEVEL_VARIANTS 20
 #define GMR_LEVEL_PUSH 32
 #define GMR_LEVEL_INTERLEAVE 64
+/* Adding GMR_LEVEL_STAGE to slot k's entry (1 <= k <= depth) stages the
+ * left-child window of the rules of level k in shared memory: a block takes
+ * runs of 2 x (256 / lanes per rule) consecutive rules, whose left children
+ * (the level is sorted by left child) lie in one window of the arena; one
+ * bulk copy (cp.async.bulk on an mbarrier) brings that window into 47 KB of
+ * shared memory while the right children are gathered, and the left children
+ * are read from there (runs whose window is larger read from global memory).
+ * That launch folds its emissions with the segmented fold.  Needs 16- or
+ * 32-byte lanes in power-of-two groups, no direct terminals, and a level
+ * that does not push; otherwise ignored.  Its waits are bounded: one that
+ * gives up is reported by gmr_engine_status (phase = -k). */
+#define GMR_LEVEL_STAGE 128
 int gmr_engine_set_level_variants(gmr_engine* e, int semiring, int B, const uint8_t* v, int n);
 int gmr_engine_get_level_variants(const gmr_engine* e, int semiring, int B, uint8_t* v, int cap, int* n);
 /* Exhaustive autotuner: times every variant on every launch (median of

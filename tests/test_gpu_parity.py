@@ -139,11 +139,42 @@ def test_wide_lanes_every_level_table(case, sr, B, monkeypatch):
     ref = oracle_columns(case["sched"], sr, case["V"], X, rows, cols)
     eng = gmr.Engine(case["plan"])
     Xw = engine_inputs(sr, X)
-    for table in ([v] * (eng.depth + 2) for v in (0, 3, 4, 10, 13, 32, 35, 45, 64, 67, 77)):
+    for table in ([v] * (eng.depth + 2) for v in (0, 3, 4, 10, 13, 32, 35, 45, 64, 67, 77, 128, 133, 138, 192)):
         eng.set_level_variants(sr, B, table)
         check(sr, eng.multiply(Xw, sr, B=B), ref)
     eng.set_level_variants(sr, B, None)
     check(sr, eng.multiply(Xw, sr, B=B, variant=gmr.VARIANT_PERSISTENT), ref)
+
+
+@pytest.fixture(scope="module")
+def staging_grammar():
+    rows, cols = 12000, 2500
+    m = gmr.gen_mosaic(rows, cols, 48, 0.01, 0.001, 41, threads=4)
+    g = gmr.repair(m, 4)
+    plan = gmr.Plan.build(g, rows, cols)
+    return dict(plan=plan, sched=O.RefSchedule(g.alpha, g.rules(), g.C()), V=g.values(), rows=rows, cols=cols)
+
+
+@pytest.mark.parametrize("sr,B", [(0, 32), (0, 128), (0, 8), (1, 256), (2, 64), (2, 4)])
+def test_staged_left_child_windows(staging_grammar, sr, B):
+    """GMR_LEVEL_STAGE on every level (left-child windows staged in shared
+    memory by bulk copies), with runs whose window fits and runs whose window
+    does not (read from global memory): every semiring matches the oracle and
+    no staged wait gave up."""
+    gd = staging_grammar
+    plan = gd["plan"]
+    words = B if sr != 1 else (B + 31) // 32
+    if words * 4 >= 128:  # values of 128 bytes or more: some runs' windows exceed the stage
+        lanes = words // (8 if sr == 0 and words >= 32 else 4)  # lanes per rule at the default lane width
+        assert plan.window_stats(2 * (256 // lanes), words)[:, 0].min() < 1.0
+    X = random_X(sr, gd["cols"], B, 900 + B)
+    ref = oracle_columns(gd["sched"], sr, gd["V"], X, gd["rows"], gd["cols"])
+    eng = gmr.Engine(plan)
+    Xw = engine_inputs(sr, X)
+    for v in (0, 2, 13):
+        eng.set_level_variants(sr, B, [v | 128] * (eng.depth + 2))
+        check(sr, engine_outputs(sr, eng.multiply(Xw, sr, B=B), B), ref)  # AUTO: the installed table
+        assert eng.status() == (0, 0)
 
 
 @pytest.mark.parametrize("sr", range(3))
@@ -251,7 +282,7 @@ def test_autotuned_and_mixed_tables(case, sr):
     times = eng.autotune(sr, dX.data_ptr(), dY.data_ptr(), B)
     assert times.shape == (eng.depth + 2, eng.N_LEVEL_VARIANTS) and np.all(times[1:] > 0)
     best = eng.level_variants(sr, B)
-    modes = gmr.LEVEL_PUSH | gmr.LEVEL_INTERLEAVE
+    modes = gmr.LEVEL_PUSH | gmr.LEVEL_INTERLEAVE | gmr.LEVEL_STAGE
     assert best is not None and np.array_equal(best[1:] & (255 - modes), times[1:].argmin(axis=1))
     assert not np.any(best[[0, eng.depth + 1]] & modes)  # only levels 1..depth push or interleave
     rng = np.random.default_rng(sr)
@@ -282,7 +313,7 @@ def test_energy_aware_autotune(case, sr):
     for slot in range(1, eng.depth + 2):
         b = int(times[slot].argmin())
         want = b + 10 if b < 10 and times[slot, b + 10] <= times[slot, b] * (1 + tol) else b
-        assert table[slot] & (255 - gmr.LEVEL_PUSH - gmr.LEVEL_INTERLEAVE) == want
+        assert table[slot] & (255 - gmr.LEVEL_PUSH - gmr.LEVEL_INTERLEAVE - gmr.LEVEL_STAGE) == want
     check(sr, engine_outputs(sr, eng.multiply(Xw, sr, B=B), B), ref)
     with pytest.raises(gmr.GmrError):
         eng.autotune(sr, dX.data_ptr(), dY.data_ptr(), B, energy_tolerance=1.5)

@@ -244,7 +244,9 @@ def test_describe_lists_levels(case):
     g = gmr.Grammar.from_arrays(int(case["alpha"]), case["rules"], case["C"], case["V"])
     d = gmr.Plan.build(g, int(case["rows"]), int(case["cols"])).describe()
     assert d.startswith("Max depth (L): ")
-    assert len([ln for ln in d.splitlines() if ln[:1].isdigit()]) == case["ref_head"][1] + 1
+    levels, windows = d.split("Left-child windows")
+    assert len([ln for ln in levels.splitlines() if ln[:1].isdigit()]) == case["ref_head"][1] + 1
+    assert len([ln for ln in windows.splitlines() if ln[:1].isdigit()]) == case["ref_head"][1]
 
 
 def test_alg_bytes_formula(case):
@@ -311,3 +313,29 @@ def test_left_edge_lists_runlength():
     p.prepare_left()
     X = np.array([[2.0], [-1.0]])
     np.testing.assert_allclose(interp_left_edges(p, 0, X), interp_left(p, 0, X), atol=1e-12)
+
+
+def test_window_stats_match_numpy_restatement():
+    """The plan's left-child window statistics (shared-memory staging) equal a
+    direct numpy computation over the plan arrays."""
+    m = gmr.gen_mosaic(4000, 900, 32, 0.02, 0.002, 5, threads=4)
+    g = gmr.repair(m, 4)
+    plan = gmr.Plan.build(g, 4000, 900)
+    R, words = 64, 8
+    got = plan.window_stats(R, words)
+    lvl, opl = plan.array("lvl_off"), plan.array("op_l")
+    assert got.shape == (plan.stats["depth"], 5)
+    for k in range(1, plan.stats["depth"] + 1):
+        a, b = int(lvl[k - 1]), int(lvl[k])
+        fits, dens, runs = np.zeros(3), [], 0
+        for r0 in range(a, b, R):
+            c = opl[r0:min(r0 + R, b)]
+            c = c[c >= 0]
+            runs += 1
+            win = (int(c[-1]) - int(c[0]) + 1) if len(c) else 0
+            fits += np.array([win * words * 4 <= x * 1024 for x in (64, 128, 200)])
+            if len(c):
+                dens.append(len(np.unique(c)) / win)
+        exp = [*(fits / max(runs, 1)), np.mean(dens) if dens else 0.0, (opl[a:b] >= 0).mean() if b > a else 0.0]
+        np.testing.assert_allclose(got[k - 1], exp, rtol=1e-12, atol=1e-12)
+    assert "Left-child windows" in plan.describe()
