@@ -349,14 +349,17 @@ def check_all_columns(sched, V, sr, Xh, Yh, rows, cols, B, threads):
     return out
 
 
-def source_hash() -> str:
+def source_hash(table: str = "") -> str:
     """Hash of the sources that make the sweep kernels: a traffic figure is
     only reported for the build it was measured on."""
     import hashlib
 
     h = hashlib.sha256()
-    for f in ("g-mm-repair_gb300/csrc/engine.cu", "g-mm-repair_gb300/csrc/device_util.cuh",
-              "g-mm-repair_gb300/csrc/gmr_internal.h", "include/gmr.h"):
+    files = ["g-mm-repair_gb300/csrc/engine.cu", "g-mm-repair_gb300/csrc/device_util.cuh",
+             "g-mm-repair_gb300/csrc/async_copy.cuh", "g-mm-repair_gb300/csrc/gmr_internal.h", "include/gmr.h"]
+    if table == "learned":  # the table the cost model picks
+        files.append("g-mm-repair_gb300/gmr/models/cost_model.gmrmlp")
+    for f in files:
         h.update((REPO / f).read_bytes())
     return h.hexdigest()[:16]
 
@@ -372,8 +375,10 @@ def traffic_entry(key: str):
         return None, f"unreadable traffic file: {e}"
     if not isinstance(ent, dict):
         return None, f"no capture for {key}"
-    if ent.get("source_hash") != source_hash():
-        return None, f"capture {ent.get('source_hash')} is of other kernel sources than this build ({source_hash()})"
+    table = key.rsplit("/", 1)[-1]
+    if ent.get("source_hash") != source_hash(table):
+        return None, (f"capture {ent.get('source_hash')} is of other kernel sources than this build "
+                      f"({source_hash(table)})")
     return ent, None
 
 
@@ -708,6 +713,41 @@ def run_other_op(args):
     return 0
 
 
+def run_launch_list(args):
+    """One eager multiply of the workload, launch by launch, with the
+    headline's per-launch table (--table learned | autotuned | default), after
+    --warmup others: the command that the ncu captures of k_level run.  Prints
+    the per-launch device times and the launch count of one multiply."""
+    import torch
+
+    import gmr
+    from gmr import learn
+
+    torch.cuda.set_device(0)
+    g, rows, cols, _ = workload_grammar(args)
+    plan = gmr.Plan.build(g, rows, cols, device=0)
+    eng = gmr.Engine(plan)
+    sr, B = SR_IDS[args.semiring], args.B
+    Xh = make_inputs(sr, cols, B, 1)
+    X = torch.from_numpy(Xh.view(np.int32)).cuda()
+    Y = torch.empty((rows, Xh.shape[1]), dtype=torch.int32, device="cuda")
+    sp = torch.cuda.current_stream().cuda_stream
+    if args.table == "learned":
+        learn.choose_learned(eng, plan, learn.Mlp.load(learn.MODEL_PATH), sr, B)
+    elif args.table == "autotuned":
+        eng.autotune(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, reps=3)
+    table = eng.level_variants(sr, B)
+    for _ in range(args.warmup):
+        eng.time_launches(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp)
+    ms = eng.time_launches(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp)
+    print(json.dumps({"op": "launches", "workload": args.workload, "semiring": args.semiring, "B": B,
+                      "table_kind": args.table, "table": None if table is None else [int(v) for v in table],
+                      "launches_per_multiply": int(eng.last_launches), "level_launches": int(eng.last_launches) - 1,
+                      "warmup_multiplies": args.warmup, "launch_ms": [round(float(t), 5) for t in ms],
+                      "source_hash": source_hash(args.table)}), flush=True)
+    return 0
+
+
 def run_gather_sweep(args):
     """The gather calibration along every load path: random 128-byte units
     (and larger units for bulk copies) from a buffer that fits in L2 (64 MB)
@@ -752,10 +792,13 @@ def main():
     ap.add_argument("--no-cusparse", action="store_true", help="skip the cuSPARSE CSR baseline")
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="--impl reference: skip timing the reference's own GPU engine beside its CPU sweep")
-    ap.add_argument("--op", choices=["right", "left", "fixpoint", "repair", "gather"], default="right",
+    ap.add_argument("--table", choices=["learned", "autotuned", "default"], default="learned",
+                    help="--op launches: the per-launch table of the multiply")
+    ap.add_argument("--op", choices=["right", "left", "fixpoint", "repair", "gather", "launches"], default="right",
                     help="right: Y = M X (the headline); left: Y = X^T M; fixpoint: X <- X (+) M X to convergence; "
                          "repair: RePair of the workload's matrix on the GPU vs the host; "
-                         "gather: the random-gather calibration along every load path")
+                         "gather: the random-gather calibration along every load path; "
+                         "launches: one eager multiply launch by launch (the ncu capture's command)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.semiring is None:
@@ -770,6 +813,8 @@ def main():
         return run_repair_compare(args)
     if args.op == "gather":
         return run_gather_sweep(args)
+    if args.op == "launches":
+        return run_launch_list(args)
     if args.op != "right":
         return run_other_op(args)
 
@@ -957,12 +1002,15 @@ def main():
     # value, every rule reads two and writes one), against the measured ceilings
     # of random 128-byte gathers from L2 and from HBM on this GPU
     vbytes = 4.0 * words * (st["n_emit"] + st["n_term_emit"] + 3 * st["n_ops"])
-    ceil_l2 = gmr.measure_gather_bandwidth(64 << 20, device=local)
-    ceil_hbm = gmr.measure_gather_bandwidth(4 << 30, device=local)
+    lane_mode = "load32" if eng.lane_bytes(sr, B) == 32 else "load16"  # the load path the sweep uses here
+    ceil_l2 = gmr.measure_gather(64 << 20, mode=lane_mode, depth=4, device=local)
+    ceil_hbm = gmr.measure_gather(4 << 30, mode=lane_mode, depth=4, device=local)
     l2_seq = gmr.measure_gather_bandwidth(64 << 20, device=local, sequential=True)
     value_gbs = vbytes / (level_ms / 1000.0) / 1e9
     step_gbs = alg_total / (ms_per_step / 1000.0) / 1e9
-    tkey = f"{args.workload}/{args.semiring}/B{B}/push{args.push}"
+    head = tuning.get("headline", "")
+    tkey = (f"{args.workload}/{args.semiring}/B{B}/"
+            f"{'learned' if head == 'learned' else 'autotuned' if head.startswith('autotuned') else 'default'}")
     traffic_ent, traffic_why = traffic_entry(tkey)
     traffic = traffic_ent["dram_bytes_per_multiply"] if traffic_ent else None
 

@@ -2096,6 +2096,18 @@ extern "C" int gmr_engine_status(const gmr_engine* e, int* failed, int* phase) {
     });
 }
 
+extern "C" int gmr_engine_lane_bytes(gmr_engine* e, int semiring, int B) {
+    if (!e || semiring < 0 || semiring > 2 || B < 1) return -1;
+    try {
+        // 256-byte aligned stand-ins: only the alignment of X and Y enters the choice
+        const Launch lc = resolve_launch(e, semiring, B, reinterpret_cast<const void*>(256),
+                                         reinterpret_cast<void*>(256), nullptr);
+        return lc.VEC * 4;
+    } catch (...) {
+        return -1;
+    }
+}
+
 extern "C" int64_t gmr_engine_last_launches(const gmr_engine* e) { return e ? e->last_launches : -1; }
 
 extern "C" int64_t gmr_engine_device_bytes(const gmr_engine* e) {

@@ -475,6 +475,10 @@ class Engine:
 
     N_LEVEL_VARIANTS = 20
 
+    def lane_bytes(self, semiring, B: int) -> int:
+        """Bytes each lane moves per value access in a default multiply of (semiring, B)."""
+        return int(lib().gmr_engine_lane_bytes(self._h, semiring_id(semiring), int(B)))
+
     def enable_left(self, plan: "Plan"):
         """Upload the reverse adjacency needed by the left product y = x^T M."""
         _check(lib().gmr_engine_enable_left(self._h, plan._h))

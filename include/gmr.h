@@ -488,6 +488,10 @@ int gmr_pack_set_mode(gmr_pack* p, int mode, int spin_limit);
 int gmr_pack_status(const gmr_pack* p, int* persistent, int* failed, int* phase);
 void gmr_pack_free(gmr_pack* p);
 
+/* Bytes each lane moves per value access in a default multiply of (semiring,
+ * B) with aligned X and Y (32, 16, 8 or 4), or -1 for a bad argument. */
+int gmr_engine_lane_bytes(gmr_engine* e, int semiring, int B);
+
 /* Kernel launches issued by the calling thread's last multiply. */
 int64_t gmr_engine_last_launches(const gmr_engine* e);
 /* Device bytes held by the engine (schedule + scratch). */

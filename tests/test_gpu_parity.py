@@ -780,3 +780,12 @@ def test_c1_boolean_tropical_bit_exact(c1):
         for b in rng.choice(B, 4, replace=False):
             ref = c1["sched"].cpu_reference(sr, c1["V"].astype(np.float32), X[:, b], 20000, 5000, threads=1)
             np.testing.assert_array_equal(Y[:, b], ref)
+
+
+def test_lane_width_rule(case):
+    """32-byte lanes for (+,x) tiles of 32 words or more, 16-byte lanes for
+    (min,+) and narrower tiles, narrower accesses where the width demands."""
+    eng = gmr.Engine(case["plan"])
+    assert [eng.lane_bytes(0, B) for B in (32, 64, 128, 8, 4, 2, 3)] == [32, 32, 32, 16, 16, 8, 4]
+    assert [eng.lane_bytes(2, B) for B in (32, 8)] == [16, 16]
+    assert [eng.lane_bytes(1, B) for B in (32, 128, 256)] == [4, 16, 16]
