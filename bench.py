@@ -917,12 +917,20 @@ def main():
             tuning["energy_table_vps"] = B * 1000.0 / timed(30)
             tuning["energy_table_mj_per_vector"] = energy_of(lambda: step_cfg(variant=0))
             eng.autotune(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, reps=3)
+
+            def slot_us():  # eager per-launch-slot device times of the installed table (median of 3)
+                runs = [eng.time_launches(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp) for _ in range(3)]
+                n = min(len(r) for r in runs)
+                return [round(float(np.median([r[i] for r in runs])) * 1000.0, 1) for i in range(n)]
+
+            tuning["autotuned_slot_us"] = slot_us()
             if learn.MODEL_PATH.exists():
                 model = learn.Mlp.load(learn.MODEL_PATH)
                 t0 = time.perf_counter()
                 learn.choose_learned(eng, plan, model, sr, B)
                 tuning["learned_choice_s"] = round(time.perf_counter() - t0, 3)
                 tuning["learned_table"] = [int(v) for v in eng.level_variants(sr, B)]
+                tuning["learned_slot_us"] = slot_us()
                 learned_ms = timed(30)
                 tuning["learned_vps"] = B * 1000.0 / learned_ms
                 tuning["learned_regret_vs_autotuner"] = learned_ms / auto_ms - 1.0

@@ -2768,20 +2768,24 @@ extern "C" int gmr_pack_multiply(gmr_pack* p, const int* semirings, const void* 
         std::vector<std::unique_lock<std::mutex>> locks;
         for (auto* e : order) locks.emplace_back(e->mu);
         DeviceGuard dg(p->device);
+        bool uniform = true, direct = false;
+        for (int i = 0; i < n; ++i) {
+            uniform = uniform && semirings[i] == semirings[0];
+            direct = direct || p->engines[i]->direct_terms;
+        }
+        // the single-kernel packings instantiate lanes of up to 16 bytes; the
+        // graph of per-engine branches runs each engine's own chain
+        const bool one_kernel = uniform && !direct &&
+                                (p->mode == GMR_PACK_PERSISTENT || (p->mode == GMR_PACK_LEVELS && n <= kMaxPackLevels));
         std::vector<Launch> lcs;
         for (int i = 0; i < n; ++i) {
             gmr_engine* e = p->engines[i];
             if (semirings[i] < 0 || semirings[i] > 2) throw Error(GMR_ERR_ARG, "unknown semiring");
             if (B[i] < 1) throw Error(GMR_ERR_ARG, "B must be >= 1");
             if (((uintptr_t)dX[i] | (uintptr_t)dY[i]) % 4 != 0) throw Error(GMR_ERR_ARG, "misaligned X or Y");
-            Launch lc = resolve_launch(e, semirings[i], B[i], dX[i], dY[i], nullptr, 4);
+            Launch lc = resolve_launch(e, semirings[i], B[i], dX[i], dY[i], nullptr, one_kernel ? 4 : 8);
             ensure_scratch(e, lc.Bw);
             lcs.push_back(lc);
-        }
-        bool uniform = true, direct = false;
-        for (int i = 0; i < n; ++i) {
-            uniform = uniform && semirings[i] == semirings[0];
-            direct = direct || p->engines[i]->direct_terms;
         }
         p->last_persistent = false;
         if (p->mode == GMR_PACK_PERSISTENT && uniform && !direct) {

@@ -5,7 +5,8 @@
 // emission and row-segment counts, emissions per segment, emission fan-out
 // (emissions per distinct source), the child-distance histogram of the
 // level's rules, the size of the previous level's values at this B, the
-// semiring and the position in the sweep.  The model input is those features
+// semiring, the position in the sweep and whether terminals are evaluated
+// in place.  The model input is those features
 // plus a one-hot of the kernel variant; the output is log(time in us).
 //
 // The model is a fully connected ReLU network, in -> 64 -> 64 -> 64 -> 1, in

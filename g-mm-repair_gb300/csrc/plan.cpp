@@ -521,6 +521,11 @@ extern "C" int gmr_plan_launch_features(const gmr_plan* p, int semiring, int B, 
         const auto& st = slot_stats(*p);
         const double words = semiring == GMR_BOOLEAN ? (double)((B + 31) / 32) : (double)B;
         std::fill(out, out + (size_t)slots * NF, 0.0f);
+        // the engine evaluates terminals in place (no terminal table) when
+        // there are more than 4 terminals per column and codes fit 31 bits
+        const int64_t n_te = p->em_off.size() > 1 ? p->em_off[1] - p->em_off[0] : 0;
+        const bool direct = n_te > 0 && p->n_terms() > 4 * (int64_t)p->cols &&
+                            (int64_t)p->V.size() * p->cols <= INT32_MAX;
         for (int k = 1; k < slots; ++k) {
             const double* s = st.data() + (size_t)k * 8;
             float* f = out + (size_t)k * NF;
@@ -539,6 +544,7 @@ extern "C" int gmr_plan_launch_features(const gmr_plan* p, int semiring, int B, 
             f[13] = (float)std::log1p((double)p->rows);
             f[14] = (float)std::log1p((double)p->n_ops());
             f[15] = (float)k / (float)(D + 1);
+            f[16] = direct ? 1.0f : 0.0f;
         }
         *n_slots = slots;
     });

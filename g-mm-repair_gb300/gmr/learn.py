@@ -27,7 +27,7 @@ import numpy as np
 from . import _lib as L
 from . import Engine, Grammar, Plan, _check, gen_copy_graph, gen_mosaic, lib, repair, semiring_id
 
-N_BASE = 16
+N_BASE = 17
 N_VAR = 20
 IN_DIM = N_BASE + N_VAR
 MODEL_PATH = Path(__file__).resolve().parent / "models" / "cost_model.gmrmlp"
@@ -160,7 +160,11 @@ def corpus_specs(n_mosaic: int, n_graph: int, seed0: int = 100, full: bool = Tru
         nodes = (int(np.exp(r.uniform(np.log(1_000_000), np.log(16_777_216)))) if full
                  else int(r.integers(200_000, 1_500_001)))
         degree = int(r.integers(8, 65)) if full else int(r.integers(8, 33))
-        specs.append(dict(kind="graph", seed=seed, nodes=nodes, degree=degree, copy=float(r.uniform(0.3, 0.9))))
+        # every other graph weighted (U{1..100} weights, as for (min,+)), the
+        # others plain adjacency (as for (OR,AND)): their terminals differ
+        # in kind (one per (weight, column) against one per column)
+        specs.append(dict(kind="graph", seed=seed, nodes=nodes, degree=degree, copy=float(r.uniform(0.3, 0.9)),
+                          weighted=i % 2 == 0))
     return specs
 
 
@@ -171,7 +175,7 @@ def make_grammar(spec, threads=0, device=None):
         m = gen_mosaic(spec["rows"], spec["cols"], spec["founders"], spec["switch"], spec["mutation"], spec["seed"],
                        threads)
         return repair(m, threads, device=device), spec["rows"], spec["cols"]
-    m = gen_copy_graph(spec["nodes"], spec["degree"], spec["copy"], True, spec["seed"], threads)
+    m = gen_copy_graph(spec["nodes"], spec["degree"], spec["copy"], spec.get("weighted", True), spec["seed"], threads)
     return repair(m, threads, device=device), spec["nodes"], spec["nodes"]
 
 
@@ -276,7 +280,12 @@ def main():
             z = np.load(done[0], allow_pickle=False)
             recs = []
             for i in range(len(z["sr"])):
-                Xin, T = training_rows(z[f"base{i}"], z[f"times{i}"])
+                base = z[f"base{i}"]
+                if base.shape[1] == N_BASE - 1:  # recorded before the in-place-terminals feature
+                    if spec["kind"] != "mosaic":
+                        raise SystemExit(f"rec_{gi}: a graph recorded without the in-place-terminals feature")
+                    base = np.concatenate([base, np.zeros((base.shape[0], 1), np.float32)], axis=1)
+                Xin, T = training_rows(base, z[f"times{i}"])
                 recs.append(dict(g=gi, sr=int(z["sr"][i]), B=int(z["B"][i]), X=Xin, T=T, times=z[f"times{i}"]))
             info = dict(grammar=gi, loaded=str(done[0]))
         else:

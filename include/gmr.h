@@ -366,8 +366,10 @@ int gmr_engine_autotune_energy(gmr_engine* e, int semiring, const void* dX, void
  *  9 log1p MB of level k-1 values at this B   10 log2 words per slot
  * 11 semiring is (OR,AND)   12 semiring is (min,+)   13 log1p rows
  * 14 log1p rules in total   15 k / (depth + 1)
+ * 16 terminals evaluated in place (the engine's default for plans with more
+ *    than 4 terminals per column, such as weighted graphs: no terminal table)
  * out: [slots][GMR_N_BASE_FEATURES]. */
-#define GMR_N_BASE_FEATURES 16
+#define GMR_N_BASE_FEATURES 17
 int gmr_plan_launch_features(const gmr_plan* p, int semiring, int B, float* out, int cap, int* n_slots);
 
 /* Fully connected ReLU network in -> hidden^layers -> 1 (fp32), trained and
