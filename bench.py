@@ -856,6 +856,9 @@ def run_launch_list(args):
         learn.choose_learned(eng, plan, learn.Mlp.load(learn.MODEL_PATH), sr, B)
     elif args.table == "autotuned":
         eng.autotune(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, reps=3)
+    elif args.table == "push":  # default variants, every level pushes its emissions into Y
+        d = plan.stats["depth"]
+        eng.set_level_variants(sr, B, [0] + [gmr.LEVEL_PUSH] * d + [0])
     table = eng.level_variants(sr, B)
     for _ in range(args.warmup):
         eng.time_launches(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp)
@@ -912,7 +915,7 @@ def main():
     ap.add_argument("--no-cusparse", action="store_true", help="skip the cuSPARSE CSR baseline")
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="--impl reference: skip timing the reference's own GPU engine beside its CPU sweep")
-    ap.add_argument("--table", choices=["learned", "autotuned", "default"], default="learned",
+    ap.add_argument("--table", choices=["learned", "autotuned", "default", "push"], default="learned",
                     help="--op launches: the per-launch table of the multiply")
     ap.add_argument("--op", choices=["right", "left", "fixpoint", "repair", "gather", "launches"], default="right",
                     help="right: Y = M X (the headline); left: Y = X^T M; fixpoint: X <- X (+) M X to convergence; "
