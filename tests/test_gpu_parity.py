@@ -115,7 +115,7 @@ CONFIGS = [
 
 
 @pytest.mark.parametrize("sr", range(3))
-@pytest.mark.parametrize("B", [2, 3, 8, 32, 33, 64, 128])
+@pytest.mark.parametrize("B", [2, 3, 8, 32, 33, 64, 128, 256])
 def test_golden_batched(case, sr, B):
     rows, cols = int(case["rows"]), int(case["cols"])
     X = random_X(sr, cols, B, 100 + B)
