@@ -1003,7 +1003,11 @@ struct gmr_engine {
     bool left_ready = false;
     int* status_host = nullptr;                           // pinned copy of the last error words
     bool last_persistent = false;  // the last multiply reported error words (persistent or staged launches)
-    int* stage_err() { return reinterpret_cast<int*>(static_cast<unsigned char*>(sync.p) + 8); }
+    // sync (64 bytes, allocated once with the engine so that captured graphs
+    // keep a valid address): [0, 8) persistent barrier, [8, 16) persistent
+    // error words, [8, 20) fixpoint flag / count / limit, [32, 40) staged-wait
+    // error words
+    int* stage_err() { return reinterpret_cast<int*>(static_cast<unsigned char*>(sync.p) + 32); }
     cudaStream_t own_stream = nullptr;
     std::vector<gmr::GraphEntry> graphs;
     std::map<std::pair<int, int>, std::vector<uint8_t>> level_variants;  // (semiring, B) -> per-launch variant
@@ -1067,6 +1071,11 @@ static bool level_staged(const gmr_engine* e, const Launch& lc, int k) {
     if (e->direct_terms || lc.VEC < 4 || (lc.G & (lc.G - 1)) != 0 || lc.G > 32) return false;
     return level_mode(e, lc, k) != kFoldPush;
 }
+
+// Set while the fixpoint loop's body is captured: its conditional body holds
+// the level kernels only, so the staged waits' error words are reset and
+// read around the whole loop instead of around each multiply.
+static thread_local bool t_chain_no_status = false;
 
 static bool any_staged(const gmr_engine* e, const Launch& lc) {
     for (int k = 1; k <= e->depth; ++k)
@@ -1288,7 +1297,7 @@ static void launch_chain_t(gmr_engine* e, const Launch& lc, const void* X, void*
         }
     };
     const int D = e->depth;
-    const bool staged = any_staged(e, lc);
+    const bool staged = any_staged(e, lc) && !t_chain_no_status;
     if (staged) GMR_CUDA(cudaMemsetAsync(e->stage_err(), 0, 8, st));  // the staged waits' error words
     if (lc.variant == GMR_VARIANT_PLAIN) {
         level(0, 0, 0, lc.ntile, true);  // terminal emissions
@@ -1768,8 +1777,8 @@ extern "C" int gmr_engine_create(const gmr_plan* p, int device, gmr_engine** out
             upload(p->lvl_off, e->d_lvl_off);
             upload(p->em_off, e->d_em_off);
             upload(p->seg_off, e->d_seg_off);
-            e->sync.ensure(16);
-            GMR_CUDA(cudaMemset(e->sync.p, 0, 16));
+            e->sync.ensure(64);
+            GMR_CUDA(cudaMemset(e->sync.p, 0, 64));
             build_chunked_emissions(*p, *e);
             GMR_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&e->status_host), 16, cudaHostAllocDefault));
             std::memset(e->status_host, 0, 16);
@@ -2099,6 +2108,7 @@ extern "C" int gmr_engine_status(const gmr_engine* e, int* failed, int* phase) {
 extern "C" int gmr_engine_lane_bytes(gmr_engine* e, int semiring, int B) {
     if (!e || semiring < 0 || semiring > 2 || B < 1) return -1;
     try {
+        std::lock_guard<std::mutex> lk(e->mu);
         // 256-byte aligned stand-ins: only the alignment of X and Y enters the choice
         const Launch lc = resolve_launch(e, semiring, B, reinterpret_cast<const void*>(256),
                                          reinterpret_cast<void*>(256), nullptr);
@@ -2456,7 +2466,14 @@ static GraphEntry* fixpoint_graph(gmr_engine* e, const Launch& lc, int semiring,
         int64_t launches = 0;
         cudaGraph_t captured = nullptr;
         try {
-            launch_chain(e, lc, X, Y, e->own_stream, launches);
+            t_chain_no_status = true;
+            try {
+                launch_chain(e, lc, X, Y, e->own_stream, launches);
+            } catch (...) {
+                t_chain_no_status = false;
+                throw;
+            }
+            t_chain_no_status = false;
             const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)e->sm_count * 8));
             if (semiring == GMR_BOOLEAN)
                 k_merge_changed<SBool><<<blocks, 256, 0, e->own_stream>>>(static_cast<uint32_t*>(X),
@@ -2508,13 +2525,18 @@ extern "C" int gmr_engine_fixpoint(gmr_engine* e, int semiring, void* dX, void* 
         int* limit = flag + 2;
         GraphEntry* g = fixpoint_graph(e, lc, semiring, dX, dY, n, flag, count, limit);
         GMR_CUDA(cudaMemsetAsync(flag, 0, 8, st));
+        GMR_CUDA(cudaMemsetAsync(e->stage_err(), 0, 8, st));
         k_set_i32<<<1, 1, 0, st>>>(limit, max_iters);
         GMR_CUDA(cudaGetLastError());
         GMR_CUDA(cudaGraphLaunch(g->exec, st));
         GMR_CUDA(cudaMemcpyAsync(e->status_host + 2, count, 4, cudaMemcpyDeviceToHost, st));
+        GMR_CUDA(cudaMemcpyAsync(e->status_host, e->stage_err(), 8, cudaMemcpyDeviceToHost, st));
         GMR_CUDA(cudaStreamSynchronize(st));
         if (iters) *iters = e->status_host[2];
         e->last_launches = g->launches * e->status_host[2] + 1;
+        if (e->status_host[0] != 0)
+            throw Error(GMR_ERR_TIMEOUT, "fixpoint: a staged-window wait gave up at level " +
+                                             std::to_string(-e->status_host[1]) + "; X is not valid");
     });
 }
 

@@ -570,6 +570,42 @@ def test_pipelined_host_multiplies(case, sr, n):
 
 
 @pytest.mark.parametrize("sr", [1, 2])
+def test_fixpoint_with_staged_levels(sr):
+    """The fixpoint loop over multiplies whose levels stage their left-child
+    windows in shared memory (GMR_LEVEL_STAGE installed for this (semiring,
+    B)): the staged launches' error words do not disturb the loop's change
+    flag and iteration count, and the result is the oracle's, bit for bit."""
+    torch = pytest.importorskip("torch")
+    c = load_case("graph_400" if sr == 1 else "graph_w300")
+    n = int(c["rows"])
+    g = gmr.Grammar.from_arrays(int(c["alpha"]), c["rules"], c["C"], c["V"])
+    eng = gmr.Engine(gmr.Plan.build(g, n, n))
+    sched = O.RefSchedule(int(c["alpha"]), c["rules"], c["C"])
+    rng = np.random.default_rng(9)
+    B = 128 if sr == 1 else 4  # 4 words per slot: 16-byte lanes, so staging applies
+    if sr == 1:
+        X = (rng.random((n, B)) < 0.01).astype(np.float32)
+    else:
+        X = np.full((n, B), 1e9, dtype=np.float32)
+        X[rng.random((n, B)) < 0.01] = 0.0
+    ref, iters_ref = X.copy(), 0
+    while True:
+        iters_ref += 1
+        Y = oracle_columns(sched, sr, c["V"], ref, n, n)
+        new = np.maximum(ref, Y) if sr == 1 else np.minimum(ref, Y)
+        if np.array_equal(new, ref):
+            break
+        ref = new
+    eng.set_level_variants(sr, B, [128] * (eng.depth + 2))
+    Xw = engine_inputs(sr, X) if sr == 1 else X.astype(np.int32)
+    dX = torch.from_numpy(Xw.view(np.int32).copy()).cuda()
+    dY = torch.empty_like(dX)
+    assert eng.fixpoint_device(sr, dX.data_ptr(), dY.data_ptr(), B) == iters_ref
+    check(sr, engine_outputs(sr, dX.cpu().numpy().view(np.uint32 if sr == 1 else np.int32), B), ref)
+    assert eng.status() == (0, 0)
+
+
+@pytest.mark.parametrize("sr", [1, 2])
 def test_fixpoint_iteration_limit_and_repeat(sr):
     """max_iters caps the device-side loop (0 runs nothing, 1 runs one merge);
     a second call on the same buffers replays the cached loop graph."""
