@@ -357,8 +357,10 @@ def source_hash(table: str = "") -> str:
     h = hashlib.sha256()
     files = ["g-mm-repair_gb300/csrc/engine.cu", "g-mm-repair_gb300/csrc/device_util.cuh",
              "g-mm-repair_gb300/csrc/async_copy.cuh", "g-mm-repair_gb300/csrc/gmr_internal.h", "include/gmr.h"]
-    if table == "learned":  # the table the cost model picks
+    if table == "learned":  # the table the cost models pick
         files.append("g-mm-repair_gb300/gmr/models/cost_model.gmrmlp")
+        if (REPO / "g-mm-repair_gb300/gmr/models/mode_model.gmrmlp").exists():
+            files.append("g-mm-repair_gb300/gmr/models/mode_model.gmrmlp")
     for f in files:
         h.update((REPO / f).read_bytes())
     return h.hexdigest()[:16]
@@ -833,6 +835,12 @@ def run_other_op(args):
     return 0
 
 
+def load_mode_model(learn):
+    """The emission-mode model, when one is committed (else the learned table
+    pulls every level's emissions)."""
+    return learn.Mlp.load(learn.MODE_MODEL_PATH) if learn.MODE_MODEL_PATH.exists() else None
+
+
 def run_launch_list(args):
     """One eager multiply of the workload, launch by launch, with the
     headline's per-launch table (--table learned | autotuned | default), after
@@ -853,7 +861,7 @@ def run_launch_list(args):
     Y = torch.empty((rows, Xh.shape[1]), dtype=torch.int32, device="cuda")
     sp = torch.cuda.current_stream().cuda_stream
     if args.table == "learned":
-        learn.choose_learned(eng, plan, learn.Mlp.load(learn.MODEL_PATH), sr, B)
+        learn.choose_learned(eng, plan, learn.Mlp.load(learn.MODEL_PATH), sr, B, mode_model=load_mode_model(learn))
     elif args.table == "autotuned":
         eng.autotune(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp, reps=3)
     elif args.table == "push":  # default variants, every level pushes its emissions into Y
@@ -1050,7 +1058,7 @@ def main():
             if learn.MODEL_PATH.exists():
                 model = learn.Mlp.load(learn.MODEL_PATH)
                 t0 = time.perf_counter()
-                learn.choose_learned(eng, plan, model, sr, B)
+                learn.choose_learned(eng, plan, model, sr, B, mode_model=load_mode_model(learn))
                 tuning["learned_choice_s"] = round(time.perf_counter() - t0, 3)
                 tuning["learned_table"] = [int(v) for v in eng.level_variants(sr, B)]
                 tuning["learned_slot_us"] = slot_us()

@@ -1011,6 +1011,10 @@ struct gmr_engine {
     cudaStream_t own_stream = nullptr;
     std::vector<gmr::GraphEntry> graphs;
     std::map<std::pair<int, int>, std::vector<uint8_t>> level_variants;  // (semiring, B) -> per-launch variant
+    // (semiring, B) -> the last autotune's per-slot times under each pair of
+    // emission modes (slot k, level k-1 in mode mp, level k in mode m: entry
+    // k * 9 + 3 * mp + m, ms; -1 where not measured)
+    std::map<std::pair<int, int>, std::vector<float>> mode_costs;
     int64_t last_launches = 0;
     int sm_count = 152;
     std::mutex mu;
@@ -2056,6 +2060,10 @@ extern "C" int gmr_engine_autotune_energy(gmr_engine* e, int semiring, const voi
                         c = c == kUnset ? tt[k] : std::min(c, tt[k]);
                     }
                 }
+            std::vector<float>& mc = e->mode_costs[{semiring, B}];
+            mc.assign((size_t)nl * 9, kUnset);
+            for (int k = 0; k < nl; ++k)
+                for (int j = 0; j < 9; ++j) mc[(size_t)k * 9 + j] = cost[k][j];
             const float kInf = 3.0e38f;
             std::vector<std::array<float, 3>> acc(D + 2);
             std::vector<std::array<int, 3>> from(D + 2);
@@ -2102,6 +2110,21 @@ extern "C" int gmr_engine_status(const gmr_engine* e, int* failed, int* phase) {
         if (!e) throw Error(GMR_ERR_ARG, "null engine");
         if (failed) *failed = e->status_host ? e->status_host[0] : 0;
         if (phase) *phase = e->status_host ? e->status_host[1] : 0;
+    });
+}
+
+extern "C" int gmr_engine_mode_costs(gmr_engine* e, int semiring, int B, float* out, int cap, int* n_slots) {
+    return guarded([&] {
+        if (!e || !out || !n_slots) throw Error(GMR_ERR_ARG, "null argument");
+        std::lock_guard<std::mutex> lk(e->mu);
+        auto it = e->mode_costs.find({semiring, B});
+        if (it == e->mode_costs.end()) {
+            *n_slots = 0;
+            return;
+        }
+        if ((size_t)cap < it->second.size()) throw Error(GMR_ERR_RANGE, "need (depth + 2) x 9 floats");
+        std::copy(it->second.begin(), it->second.end(), out);
+        *n_slots = (int)(it->second.size() / 9);
     });
 }
 

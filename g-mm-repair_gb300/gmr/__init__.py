@@ -475,6 +475,16 @@ class Engine:
 
     N_LEVEL_VARIANTS = 20
 
+    def mode_costs(self, semiring, B: int):
+        """[slots][3 prev mode][3 mode] ms of the last autotune's emission-mode
+        chain search for (semiring, B) (-1 = not measured), or None."""
+        cap = (self.depth + 2) * 9
+        out = np.zeros(cap, dtype=np.float32)
+        n = C.c_int()
+        _check(lib().gmr_engine_mode_costs(self._h, semiring_id(semiring), int(B), out.ctypes.data_as(L.F32P), cap,
+                                           C.byref(n)))
+        return out[: n.value * 9].reshape(n.value, 3, 3) if n.value else None
+
     def lane_bytes(self, semiring, B: int) -> int:
         """Bytes each lane moves per value access in a default multiply of (semiring, B)."""
         return int(lib().gmr_engine_lane_bytes(self._h, semiring_id(semiring), int(B)))

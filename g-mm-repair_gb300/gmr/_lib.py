@@ -129,6 +129,7 @@ _SIGS = {
     "gmr_engine_multiply_left": (C.c_int, [P, C.c_int, P, P, C.c_int, P]),
     "gmr_engine_fixpoint": (C.c_int, [P, C.c_int, P, P, C.c_int, C.c_int, P, C.POINTER(C.c_int)]),
     "gmr_engine_lane_bytes": (C.c_int, [P, C.c_int, C.c_int]),
+    "gmr_engine_mode_costs": (C.c_int, [P, C.c_int, C.c_int, F32P, C.c_int, C.POINTER(C.c_int)]),
     "gmr_pack_create": (C.c_int, [C.POINTER(P), C.c_int, C.POINTER(P)]),
     "gmr_pack_multiply": (C.c_int, [P, C.POINTER(C.c_int), C.POINTER(P), C.POINTER(P), C.POINTER(C.c_int), P]),
     "gmr_pack_last_launches": (C.c_int64, [P]),

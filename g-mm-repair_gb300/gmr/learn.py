@@ -31,6 +31,13 @@ N_BASE = 17
 N_VAR = 20
 IN_DIM = N_BASE + N_VAR
 MODEL_PATH = Path(__file__).resolve().parent / "models" / "cost_model.gmrmlp"
+# Emission-mode model: per launch slot, log(time) given the slot's features and
+# whether level k-1 and level k are interleaved (pull otherwise).
+MODE_MODEL_PATH = Path(__file__).resolve().parent / "models" / "mode_model.gmrmlp"
+MODE_IN = N_BASE + 2
+PULL, INTERLEAVE = 0, 2           # the engine's mode indices (1 = push, not learned: it loses)
+CHUNK_SLOTS = 1 << 19             # source slots per chunk (the engine's default)
+MODE_DOMAIN = "(+,x), B >= 32"    # where the mode model was trained and is applied
 
 
 def launch_features(plan: Plan, semiring, B: int) -> np.ndarray:
@@ -122,13 +129,101 @@ class Mlp:
         return float(loss.value)
 
 
-def choose_learned(eng: Engine, plan: Plan, model: Mlp, semiring, B: int) -> np.ndarray:
-    """Installs the model's per-launch choice; returns its predictions [slots][variants] (log us)."""
+def choose_learned(eng: Engine, plan: Plan, model: Mlp, semiring, B: int, mode_model: Mlp | None = None) -> np.ndarray:
+    """Installs the model's per-launch choice; returns its predictions [slots][variants] (log us).
+    With mode_model (applied in its training domain, (+,x) at B >= 32), the
+    levels it predicts faster interleaved get GMR_LEVEL_INTERLEAVE."""
     slots = plan.stats["depth"] + 2
     pred = np.zeros(slots * N_VAR, dtype=np.float32)
     _check(lib().gmr_engine_choose_learned(eng._h, plan._h, model._h, semiring_id(semiring), B,
                                            pred.ctypes.data_as(L.F32P), len(pred)))
+    if mode_model is not None and semiring_id(semiring) == 0 and B >= 32:
+        modes = choose_modes(plan, mode_model, semiring, B)
+        table = eng.level_variants(semiring, B)
+        for k, m in enumerate(modes):
+            if m == INTERLEAVE:
+                table[k] |= 64  # GMR_LEVEL_INTERLEAVE
+        eng.set_level_variants(semiring, B, table)
     return pred.reshape(slots, N_VAR)
+
+
+def interleave_allowed(plan: Plan, chunk_slots: int = CHUNK_SLOTS) -> np.ndarray:
+    """[slots] bool: level k can run in source chunks (two chunks or more)."""
+    lvl = plan.array("lvl_off")
+    d = plan.stats["depth"]
+    ok = np.zeros(d + 2, dtype=bool)
+    for k in range(1, d + 1):
+        ok[k] = lvl[k] - lvl[k - 1] > chunk_slots
+    return ok
+
+
+def mode_inputs(base: np.ndarray, mp: int, m: int) -> np.ndarray:
+    """[slots][18]: base features + (level k-1 interleaved, level k interleaved)."""
+    x = np.zeros((base.shape[0], MODE_IN), dtype=np.float32)
+    x[:, :N_BASE] = base
+    x[:, N_BASE] = 1.0 if mp == INTERLEAVE else 0.0
+    x[:, N_BASE + 1] = 1.0 if m == INTERLEAVE else 0.0
+    return x
+
+
+def best_chain(cost, allowed) -> tuple[list, float]:
+    """The cheapest choice of pull / interleave per level: cost[k][mp][m] (any
+    array indexable so; NaN or <= 0 = not available) for slots 1..D+1, level
+    D+1 (the final fold) pulled.  Returns (mode per slot, total)."""
+    n = len(allowed)
+    inf = float("inf")
+    acc = {PULL: 0.0, INTERLEAVE: inf}
+    back = []
+    for k in range(1, n):
+        last = k == n - 1
+        nxt, frm = {}, {}
+        for m in (PULL, INTERLEAVE):
+            if m == INTERLEAVE and (last or not allowed[k]):
+                nxt[m] = inf
+                continue
+            best, arg = inf, PULL
+            for mp in (PULL, INTERLEAVE):
+                c = cost[k][mp][m]
+                if acc[mp] == inf or not np.isfinite(c) or c <= 0:
+                    continue
+                if acc[mp] + c < best:
+                    best, arg = acc[mp] + c, mp
+            nxt[m], frm[m] = best, arg
+        back.append(frm)
+        acc = nxt
+    modes = [PULL] * n
+    m = PULL
+    for k in range(n - 1, 0, -1):
+        modes[k] = m
+        m = back[k - 1].get(m, PULL)
+    return modes, acc[PULL]
+
+
+def choose_modes(plan: Plan, mode_model: Mlp, semiring, B: int) -> list:
+    """Emission mode per launch slot (PULL / INTERLEAVE) from the mode model's
+    predicted slot times, by the autotuner's chain recursion."""
+    base = launch_features(plan, semiring, B)
+    n = base.shape[0]
+    cost = np.full((n, 3, 3), np.nan)
+    for mp in (PULL, INTERLEAVE):
+        for m in (PULL, INTERLEAVE):
+            cost[:, mp, m] = np.exp(mode_model.predict(mode_inputs(base, mp, m)))
+    return best_chain(cost, interleave_allowed(plan))[0]
+
+
+def mode_rows(base: np.ndarray, costs: np.ndarray):
+    """Training rows of the mode model from one autotune's mode costs [slots][3][3] (ms)."""
+    X, T = [], []
+    for mp in (PULL, INTERLEAVE):
+        for m in (PULL, INTERLEAVE):
+            c = costs[:, mp, m]
+            keep = (np.arange(len(c)) >= 1) & (c > 0)
+            if keep.any():
+                X.append(mode_inputs(base, mp, m)[keep])
+                T.append(np.log(c[keep] * 1000.0).astype(np.float32))
+    if not X:
+        return np.zeros((0, MODE_IN), np.float32), np.zeros(0, np.float32)
+    return np.concatenate(X), np.concatenate(T)
 
 
 # ---------------------------------------------------------------- corpus
@@ -248,6 +343,82 @@ def plain_time(eng: Engine, semiring: int, B: int, seed: int, n: int = 5) -> flo
     return a.elapsed_time(b) / n
 
 
+def run_modes(args, specs, hold, out: Path):
+    """Records the autotuner's emission-mode costs on the corpus mosaics at
+    (+,x) and the given B, trains the mode model, and evaluates on the
+    held-out mosaics: the regret of its chain against the measured best chain
+    of pull / interleave, and its gain over pulling every level."""
+    import torch
+
+    Bs = [int(b) for b in args.Bs.split(",")]
+    tr_X, tr_T, held = [], [], []
+    t0 = time.time()
+    for gi, spec in enumerate(specs):
+        if spec["kind"] != "mosaic":
+            continue
+        f = out / f"rec_modes_{gi}.npz"
+        if f.exists():
+            z = np.load(f)
+            recs = [(z[f"base{i}"], z[f"costs{i}"], z[f"allowed{i}"]) for i in range(len(z["B"]))]
+        else:
+            g, rows, cols = make_grammar(spec, device=0)
+            plan = Plan.build(g, rows, cols, device=0)
+            eng = Engine(plan)
+            recs = []
+            for B in Bs:
+                X, words = random_inputs(torch, 0, cols, B, 1000 * gi + B)
+                Y = torch.empty((rows, words), device="cuda", dtype=X.dtype)
+                eng.autotune(0, X.data_ptr(), Y.data_ptr(), B, stream=torch.cuda.current_stream().cuda_stream)
+                costs = eng.mode_costs(0, B)
+                if costs is None:  # no level of this grammar can interleave or push
+                    costs = np.full((plan.stats["depth"] + 2, 3, 3), -1.0, np.float32)
+                recs.append((launch_features(plan, 0, B), costs, interleave_allowed(plan)))
+            arrays = {"B": np.array(Bs)}
+            for i, (b, c, a) in enumerate(recs):
+                arrays.update({f"base{i}": b, f"costs{i}": c, f"allowed{i}": a})
+            np.savez_compressed(f, **arrays)
+            del eng
+        for base, costs, allowed in recs:
+            if gi in hold:
+                held.append((base, costs, allowed))
+            else:
+                x, t = mode_rows(base, costs)
+                tr_X.append(x)
+                tr_T.append(t)
+        print(json.dumps(dict(grammar=gi, held_out=gi in hold, elapsed_s=round(time.time() - t0, 1))), flush=True)
+    X, T = np.concatenate(tr_X), np.concatenate(tr_T)
+    model = Mlp.create(in_dim=MODE_IN, seed=2)
+    mean, std = X.mean(axis=0), X.std(axis=0)
+    std[std < 1e-6] = 1.0
+    model.set_norm(mean, std)
+    loss = model.train(X, T, epochs=args.mode_epochs, batch=256, lr=2e-3, seed=5)
+    model.save(out / "mode_model.gmrmlp")
+    regrets, gains = [], []
+    for base, costs, allowed in held:
+        meas = np.where(costs > 0, costs, np.nan)
+        if not np.isfinite(meas[:, PULL, PULL][1:]).all():
+            continue
+        _, t_best = best_chain(meas, allowed)
+        pred = np.full(costs.shape, np.nan)
+        for mp in (PULL, INTERLEAVE):
+            for m in (PULL, INTERLEAVE):
+                pred[:, mp, m] = np.exp(model.predict(mode_inputs(base, mp, m)))
+        modes, _ = best_chain(pred, allowed)
+        t_pick = sum(meas[k][modes[k - 1]][modes[k]] for k in range(1, len(modes)))
+        if not np.isfinite(t_pick):  # a pair the autotuner did not measure: count it as pulling
+            modes = [PULL] * len(modes)
+            t_pick = np.nansum(meas[1:, PULL, PULL])
+        t_pull = np.nansum(meas[1:, PULL, PULL])
+        regrets.append(t_pick / t_best - 1.0)
+        gains.append(t_pull / t_pick)
+    report = dict(train_rows=int(len(X)), train_mse=loss, heldout_cases=len(regrets),
+                  regret_mean=float(np.mean(regrets)), regret_p90=float(np.percentile(regrets, 90)),
+                  gain_vs_all_pull_mean=float(np.mean(gains)), record_s=round(time.time() - t0, 1), Bs=Bs,
+                  domain=MODE_DOMAIN)
+    (out / "mode_report.json").write_text(json.dumps(report, indent=1))
+    print(json.dumps(report), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
@@ -257,6 +428,10 @@ def main():
     ap.add_argument("--Bs", default="1,8,32,128")
     ap.add_argument("--epochs", type=int, default=80)
     ap.add_argument("--small", action="store_true", help="the earlier small size ranges")
+    ap.add_argument("--modes", action="store_true",
+                    help="record the emission-mode costs of the corpus mosaics at (+,x) and --Bs, and train the mode "
+                         "model instead of the variant model")
+    ap.add_argument("--mode-epochs", type=int, default=300)
     ap.add_argument("--resume", default=None,
                     help="a directory holding rec_<grammar>.npz files of an earlier run: those grammars are loaded, "
                          "not recorded again")
@@ -269,6 +444,8 @@ def main():
     order = rng.permutation(len(specs))
     n_hold = int(round(len(specs) * args.holdout))
     hold = set(order[:n_hold].tolist())
+    if args.modes:
+        return run_modes(args, specs, hold, out)
     rows_tr, rows_te = [], []
     t0 = time.time()
     for gi, spec in enumerate(specs):

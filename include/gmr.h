@@ -490,6 +490,14 @@ int gmr_pack_set_mode(gmr_pack* p, int mode, int spin_limit);
 int gmr_pack_status(const gmr_pack* p, int* persistent, int* failed, int* phase);
 void gmr_pack_free(gmr_pack* p);
 
+/* The last gmr_engine_autotune of (semiring, B): each launch slot's time
+ * (ms) under each pair of emission modes, out[k * 9 + 3 * mp + m] for slot k
+ * with level k-1 in mode mp and level k in mode m (0 pulled, 1 pushed,
+ * 2 interleaved; the variants are the autotuner's per-slot choice), -1 where
+ * that pair was not measured.  *n_slots = depth + 2, or 0 when no autotune
+ * of (semiring, B) has measured the modes. */
+int gmr_engine_mode_costs(gmr_engine* e, int semiring, int B, float* out, int cap, int* n_slots);
+
 /* Bytes each lane moves per value access in a default multiply of (semiring,
  * B) with aligned X and Y (32, 16, 8 or 4), or -1 for a bad argument. */
 int gmr_engine_lane_bytes(gmr_engine* e, int semiring, int B);

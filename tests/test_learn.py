@@ -141,3 +141,46 @@ def test_learned_choice_keeps_results(name):
     assert table is not None and np.array_equal(table[1:], pred[1:].argmin(axis=1))
     Y = eng.multiply(X, 0, B=32)  # AUTO: the learned table
     np.testing.assert_allclose(Y, ref, rtol=1e-5, atol=1e-5)
+
+
+def test_mode_chain_recursion_matches_brute_force():
+    """best_chain (the mode model's choice of pull / interleave per level)
+    finds the cheapest chain that exhaustive enumeration finds, with levels
+    that cannot interleave and unmeasured pairs respected."""
+    import itertools
+
+    rng = np.random.default_rng(4)
+    for trial in range(40):
+        n = int(rng.integers(3, 9))  # slots: prologue, levels 1..n-2, final fold
+        cost = rng.uniform(1.0, 10.0, (n, 3, 3))
+        allowed = rng.random(n) < 0.6
+        allowed[0] = allowed[-1] = False
+        if trial % 3 == 0:
+            cost[rng.integers(1, n), Lr.INTERLEAVE, Lr.PULL] = np.nan  # a pair never measured
+        modes, total = Lr.best_chain(cost, allowed)
+        best = np.inf
+        for combo in itertools.product((Lr.PULL, Lr.INTERLEAVE), repeat=n - 2):
+            ms = [Lr.PULL, *combo, Lr.PULL]
+            if any(m == Lr.INTERLEAVE and not allowed[k] for k, m in enumerate(ms)):
+                continue
+            t = sum(cost[k][ms[k - 1]][ms[k]] for k in range(1, n))
+            if np.isfinite(t):
+                best = min(best, t)
+        assert np.isclose(total, best)
+        assert np.isclose(sum(cost[k][modes[k - 1]][modes[k]] for k in range(1, n)), total)
+        assert all(m == Lr.PULL or allowed[k] for k, m in enumerate(modes))
+
+
+def test_mode_rows_use_measured_pairs_only():
+    base = np.arange(4 * Lr.N_BASE, dtype=np.float32).reshape(4, Lr.N_BASE)
+    costs = np.full((4, 3, 3), -1.0, np.float32)
+    costs[1, Lr.PULL, Lr.PULL] = 0.5
+    costs[2, Lr.PULL, Lr.INTERLEAVE] = 2.0
+    costs[3, Lr.INTERLEAVE, Lr.PULL] = 1.0
+    costs[0, Lr.PULL, Lr.PULL] = 9.0  # the prologue slot is never a training row
+    X, T = Lr.mode_rows(base, costs)
+    assert X.shape == (3, Lr.MODE_IN)
+    got = {(tuple(x[Lr.N_BASE:]), float(x[0])): t for x, t in zip(X, T)}
+    assert np.isclose(got[((0.0, 0.0), float(base[1, 0]))], np.log(500.0))
+    assert np.isclose(got[((0.0, 1.0), float(base[2, 0]))], np.log(2000.0))
+    assert np.isclose(got[((1.0, 0.0), float(base[3, 0]))], np.log(1000.0))

@@ -49,7 +49,8 @@ def test_learned_tables_gain_over_default_and_regret(engine):
     for sr, B in CASES:
         seed = 10 * sr + B
         d = min(learn.sweep_time(eng, sr, B, None, seed, n=20) for _ in range(3))
-        pred = learn.choose_learned(eng, plan, model, sr, B)
+        mode_model = learn.Mlp.load(learn.MODE_MODEL_PATH) if learn.MODE_MODEL_PATH.exists() else None
+        pred = learn.choose_learned(eng, plan, model, sr, B, mode_model=mode_model)
         table = eng.level_variants(sr, B)
         lt = min(learn.sweep_time(eng, sr, B, table, seed, n=20) for _ in range(3))
         t_default += d
