@@ -412,9 +412,10 @@ def run_modes(args, specs, hold, out: Path):
         regrets.append(t_pick / t_best - 1.0)
         gains.append(t_pull / t_pick)
     report = dict(train_rows=int(len(X)), train_mse=loss, heldout_cases=len(regrets),
-                  regret_mean=float(np.mean(regrets)), regret_p90=float(np.percentile(regrets, 90)),
-                  gain_vs_all_pull_mean=float(np.mean(gains)), record_s=round(time.time() - t0, 1), Bs=Bs,
-                  domain=MODE_DOMAIN)
+                  regret_mean=float(np.mean(regrets)) if regrets else None,
+                  regret_p90=float(np.percentile(regrets, 90)) if regrets else None,
+                  gain_vs_all_pull_mean=float(np.mean(gains)) if gains else None,
+                  record_s=round(time.time() - t0, 1), Bs=Bs, domain=MODE_DOMAIN)
     (out / "mode_report.json").write_text(json.dumps(report, indent=1))
     print(json.dumps(report), flush=True)
 
