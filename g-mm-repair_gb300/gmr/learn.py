@@ -25,7 +25,7 @@ from pathlib import Path
 import numpy as np
 
 from . import _lib as L
-from . import Engine, Grammar, Plan, _check, gen_copy_graph, gen_mosaic, lib, repair, semiring_id
+from . import LEVEL_INTERLEAVE, Engine, Grammar, Plan, _check, gen_copy_graph, gen_mosaic, lib, repair, semiring_id
 
 N_BASE = 17
 N_VAR = 20
@@ -142,7 +142,7 @@ def choose_learned(eng: Engine, plan: Plan, model: Mlp, semiring, B: int, mode_m
         table = eng.level_variants(semiring, B)
         for k, m in enumerate(modes):
             if m == INTERLEAVE:
-                table[k] |= 64  # GMR_LEVEL_INTERLEAVE
+                table[k] |= LEVEL_INTERLEAVE
         eng.set_level_variants(semiring, B, table)
     return pred.reshape(slots, N_VAR)
 
