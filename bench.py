@@ -867,6 +867,9 @@ def run_launch_list(args):
     elif args.table == "push":  # default variants, every level pushes its emissions into Y
         d = plan.stats["depth"]
         eng.set_level_variants(sr, B, [0] + [gmr.LEVEL_PUSH] * d + [0])
+    elif args.table == "stage":  # default variants, every level stages its left-child windows
+        d = plan.stats["depth"]
+        eng.set_level_variants(sr, B, [0] + [gmr.LEVEL_STAGE] * d + [0])
     table = eng.level_variants(sr, B)
     for _ in range(args.warmup):
         eng.time_launches(sr, X.data_ptr(), Y.data_ptr(), B, stream=sp)
@@ -923,7 +926,7 @@ def main():
     ap.add_argument("--no-cusparse", action="store_true", help="skip the cuSPARSE CSR baseline")
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="--impl reference: skip timing the reference's own GPU engine beside its CPU sweep")
-    ap.add_argument("--table", choices=["learned", "autotuned", "default", "push"], default="learned",
+    ap.add_argument("--table", choices=["learned", "autotuned", "default", "push", "stage"], default="learned",
                     help="--op launches: the per-launch table of the multiply")
     ap.add_argument("--op", choices=["right", "left", "fixpoint", "repair", "gather", "launches"], default="right",
                     help="right: Y = M X (the headline); left: Y = X^T M; fixpoint: X <- X (+) M X to convergence; "
