@@ -428,6 +428,7 @@ def main():
     ap.add_argument("--holdout", type=float, default=0.25)
     ap.add_argument("--Bs", default="1,8,32,128")
     ap.add_argument("--epochs", type=int, default=80)
+    ap.add_argument("--seed", type=int, default=1, help="initialisation seed of the variant model")
     ap.add_argument("--small", action="store_true", help="the earlier small size ranges")
     ap.add_argument("--modes", action="store_true",
                     help="record the emission-mode costs of the corpus mosaics at (+,x) and --Bs, and train the mode "
@@ -486,7 +487,7 @@ def main():
         print(json.dumps(info | dict(held_out=gi in hold, elapsed_s=round(time.time() - t0, 1))), flush=True)
     Xtr = np.concatenate([r["X"] for r in rows_tr])
     Ttr = np.concatenate([r["T"] for r in rows_tr])
-    model = Mlp.create(seed=1)
+    model = Mlp.create(seed=args.seed)
     mean, std = Xtr.mean(axis=0), Xtr.std(axis=0)
     std[std < 1e-6] = 1.0
     model.set_norm(mean, std)
