@@ -339,3 +339,27 @@ def test_window_stats_match_numpy_restatement():
         exp = [*(fits / max(runs, 1)), np.mean(dens) if dens else 0.0, (opl[a:b] >= 0).mean() if b > a else 0.0]
         np.testing.assert_allclose(got[k - 1], exp, rtol=1e-12, atol=1e-12)
     assert "Left-child windows" in plan.describe()
+
+
+def test_window_stats_rejects_bad_arguments():
+    m = gmr.gen_mosaic(500, 200, 8, 0.02, 0.002, 3, threads=2)
+    plan = gmr.Plan.build(gmr.repair(m, 2), 500, 200)
+    with pytest.raises(gmr.GmrError):
+        plan.window_stats(0, 32)
+    with pytest.raises(gmr.GmrError):
+        plan.window_stats(64, 0)
+
+
+def test_interleave_eligibility_follows_level_widths():
+    """A level can be interleaved when it spans two source chunks or more."""
+    from gmr import learn
+
+    m = gmr.gen_mosaic(3000, 700, 16, 0.02, 0.002, 4, threads=2)
+    plan = gmr.Plan.build(gmr.repair(m, 2), 3000, 700)
+    lvl = plan.array("lvl_off")  # lvl_off[k] = end of level k, lvl_off[0] = 0
+    widths = np.diff(lvl)        # widths[k - 1] = rules of level k
+    cs = int(np.median(widths[widths > 0]))
+    ok = learn.interleave_allowed(plan, chunk_slots=cs)
+    assert not ok[0] and not ok[-1]
+    for k in range(1, plan.stats["depth"] + 1):
+        assert ok[k] == (widths[k - 1] > cs)
